@@ -1,0 +1,404 @@
+#!/usr/bin/env python3
+"""Benchmark: direction-optimizing BFS with path counts on RMAT scale 22.
+
+Workload: RMAT scale 22, edgefactor 16 (a/b/c/d = .57/.19/.19/.05, vertex ids
+permuted, symmetrised, self-loops and duplicates removed: n = 4,194,304,
+128.3M CSC entries), 64 seeded roots drawn from the giant component.  One
+step = one BFS (depth S int32 + path counts sigma int64) from each of the 64
+roots.  Metric: GTEPS = sum over roots of the undirected edges in the root's
+component / time.
+
+  value     device-timed (CUDA events on the launching stream, graph
+            resident in HBM, outputs written to HBM)
+  e2e       the same through the C ABI with host buffers: every step uploads
+            the CSC from pinned host memory, runs the 64 traversals and
+            copies every S and sigma back to pinned host memory
+  roofline  the persistent BFS kernel: algorithmic bytes per traversal
+            (4*nnz_c + 8*n_c + 12*n) / its mean CUDA-event duration, against
+            the measured HBM copy bandwidth
+  cpu_baseline  the reference's sequential BFS algorithm (oracle restatement)
+            on the host cores, one BFS per core, on a sample of the roots
+
+--impl reference times that CPU algorithm alone on this workload.
+Under torchrun (N > 1) every rank runs the same workload on its own GPU
+(replicas; BFS from a single source does not shard without a per-level
+exchange) and value is the sum over ranks of the work / the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GTEPS (undirected edges in the root's component / BFS time), direction-optimizing BFS with path counts"
+UNIT = "GTEPS"
+WORKLOAD = "rmat22_do_bfs_sigma_64roots"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["tbfs", "reference"], default="tbfs")
+    p.add_argument("--scale", type=int, default=22)
+    p.add_argument("--roots", type=int, default=64)
+    p.add_argument("--mode", default="auto")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--cpu-threads", type=int, default=0)
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_workload(scale: int, nroots: int):
+    from turbobfs_gb300 import graphs
+
+    h = graphs.rmat(scale, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    roots = graphs.pick_roots(h, nroots, seed=1)
+    return h, roots
+
+
+def config(h, nroots, world, extra=None):
+    c = {
+        "workload": WORKLOAD if h.n == 1 << 22 else f"rmat{int(np.log2(h.n))}_do_bfs_sigma_{nroots}roots",
+        "graph": "RMAT scale %d, edgefactor 16, a/b/c/d=.57/.19/.19/.05, permuted, symmetrised, "
+                 "no self-loops, deduplicated" % int(np.log2(h.n)),
+        "n": h.n,
+        "nnz": h.nnz,
+        "roots": nroots,
+        "root_seed": 1,
+        "graph_seed": 1,
+        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+        "l2": "inputs larger than L2 (CSC row_idx %d MB vs 126 MB L2); no flush" % (h.nnz * 4 // 2**20),
+    }
+    if extra:
+        c.update(extra)
+    return c
+
+
+def cpu_threads(requested: int) -> int:
+    n = requested if requested > 0 else (os.cpu_count() or 1)
+    return max(1, min(n, 64))
+
+
+def lscpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def cpu_baseline(h, roots, threads: int) -> dict:
+    import oracle
+
+    sample = roots[:threads]
+    wall, secs, edges = oracle.seq_many(h.col_ptr, h.row_idx, sample, threads)
+    gteps = float(edges.sum() / 2 / wall / 1e9)
+    return {"value": gteps, "unit": UNIT, "cores": int(threads), "kind": "port",
+            "sample": f"{len(sample)} of the {len(roots)} roots, one single-threaded BFS per "
+                      f"core at a time ({lscpu_model()}); wall {wall:.2f} s, "
+                      f"mean {float(np.mean(secs)):.2f} s per BFS",
+            "algorithm": "restatement of TurboBFS_CSC_TDBU/bfstdcsc_seq.c (int sigma)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        for line in (getattr(self, "out", "") or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        busy = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(scale: int):
+    """dram bytes (read + write) per traversal from the committed ncu summary."""
+    f = ROOT / "profiles" / f"bfs_persistent_kernel_rmat{scale}.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    h, roots = make_workload(args.scale, args.roots)
+    threads = cpu_threads(args.cpu_threads)
+    import oracle
+
+    sample = roots[:threads]
+    for _ in range(args.warmup):
+        oracle.seq_many(h.col_ptr, h.row_idx, sample, threads)
+    walls, edges_total = [], 0
+    for _ in range(args.steps):
+        wall, secs, edges = oracle.seq_many(h.col_ptr, h.row_idx, sample, threads)
+        walls.append(wall)
+        edges_total += int(edges.sum())
+    t = sum(walls)
+    value = edges_total / 2 / t / 1e9
+    cb = {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"each step: {len(sample)} of the {len(roots)} roots, one single-threaded "
+                    f"BFS per core at a time ({lscpu_model()})",
+          "algorithm": "restatement of TurboBFS_CSC_TDBU/bfstdcsc_seq.c (int sigma)"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic (seeded RMAT generator)", "impl": "reference",
+            "config": config(h, args.roots, 1, {"sample_roots_per_step": len(sample)}),
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_tbfs(args, world, rank, local):
+    import torch
+
+    import turbobfs_gb300 as tb
+    from turbobfs_gb300 import _lib
+    from turbobfs_gb300.api import _P_I32, _P_I64, make_options
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    h, roots = make_workload(args.scale, args.roots)
+    k = int(roots.shape[0])
+    n = h.n
+    g = tb.Graph.from_host_csc(h)
+    S_dev = torch.empty((k, n), dtype=torch.int32, device="cuda")
+    sg_dev = torch.empty((k, n), dtype=torch.int64, device="cuda")
+    o = make_options(args.mode, True, outputs_on_device=True)
+    stats = (_lib.Stats * k)()
+    roots_c = np.ascontiguousarray(roots, dtype=np.int32)
+    import ctypes
+
+    def step():
+        _lib.check(tb.lib().tbfs_bfs_many(
+            g.handle, roots_c.ctypes.data_as(_P_I32), k, ctypes.byref(o),
+            ctypes.cast(S_dev.data_ptr(), _P_I32), ctypes.cast(sg_dev.data_ptr(), _P_I64),
+            stats), "tbfs_bfs_many")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    edges_per_step = sum(stats[i].edges for i in range(k))
+    per_root = [stats[i].as_dict() for i in range(k)]
+    barrier()
+    launch_ms = []
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record()
+        for _ in range(args.steps):
+            step()
+            launch_ms += [stats[i].device_ms for i in range(k)]
+        e1.record()
+        barrier()
+    t_ms = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([t_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    units = world * args.steps * edges_per_step / 2
+    value = units / (t_ms / 1e3) / 1e9
+
+    # roofline of the persistent BFS kernel
+    alg_bytes = []
+    for i in range(k):
+        visited = int(per_root[i]["visited"])
+        alg_bytes.append(4 * per_root[i]["edges"] + 8 * visited + 12 * n)
+    mean_bytes = float(np.mean(alg_bytes))
+    mean_launch_ms = float(np.mean(launch_ms))
+    achieved = mean_bytes / (mean_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = traffic_per_launch(args.scale)
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(h, roots_c, args.steps, o, edges_per_step, world)
+
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(h, roots, cpu_threads(args.cpu_threads))
+    levels = [r["levels"] for r in per_root]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+        "data": "synthetic (seeded RMAT generator; no public dataset named)",
+        "impl": "tbfs",
+        "config": config(h, k, world, {"mode": args.mode, "outputs": "S int32 + sigma int64 in HBM",
+                                       "levels_min_max": [min(levels), max(levels)],
+                                       "td_bu_levels_root0": [per_root[0]["td_levels"],
+                                                              per_root[0]["bu_levels"]]}),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "bfs_persistent_kernel",
+                     "algorithmic_bytes_per_launch": mean_bytes,
+                     "mean_launch_ms": mean_launch_ms,
+                     "peak_source": f"{peak_kind} hbm_gbs"},
+        "gpu_launches": args.steps * k,
+        "clocks": clk.summary(),
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if cb:
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
+    """Public C ABI with host buffers: upload the CSC from pinned memory,
+    traverse from every root, copy all S and sigma rows back to pinned memory."""
+    import ctypes
+
+    import turbobfs_gb300 as tb
+    from turbobfs_gb300 import _lib
+    from turbobfs_gb300.api import _P_I32, _P_I64, make_options
+
+    L = tb.lib()
+    k, n, nnz = int(roots_c.shape[0]), h.n, h.nnz
+
+    def pinned(nbytes):
+        p = ctypes.c_void_p()
+        _lib.check(L.tbfs_host_alloc_pinned(nbytes, ctypes.byref(p)), "pinned")
+        return p
+
+    bufs = []
+    try:
+        p_cp, p_ic = pinned(4 * (n + 1)), pinned(4 * nnz)
+        p_S, p_sg = pinned(4 * k * n), pinned(8 * k * n)
+        bufs = [p_cp, p_ic, p_S, p_sg]
+        cp = np.ctypeslib.as_array(ctypes.cast(p_cp, _P_I32), shape=(n + 1,))
+        ic = np.ctypeslib.as_array(ctypes.cast(p_ic, _P_I32), shape=(nnz,))
+        cp[:] = h.col_ptr
+        ic[:] = h.row_idx
+        o = make_options("auto", True)
+        o.alpha, o.beta, o.mode = o_dev.alpha, o_dev.beta, o_dev.mode
+        stats = (_lib.Stats * k)()
+
+        def one():
+            hdl = ctypes.c_void_p()
+            _lib.check(L.tbfs_graph_create_csc(ctypes.cast(p_cp, _P_I32), ctypes.cast(p_ic, _P_I32),
+                                               n, nnz, _lib.GRAPH_SYMMETRIC, ctypes.byref(hdl)),
+                       "tbfs_graph_create_csc")
+            try:
+                _lib.check(L.tbfs_bfs_many(hdl, roots_c.ctypes.data_as(_P_I32), k, ctypes.byref(o),
+                                           ctypes.cast(p_S, _P_I32), ctypes.cast(p_sg, _P_I64),
+                                           stats), "tbfs_bfs_many")
+            finally:
+                L.tbfs_graph_destroy(hdl)
+
+        one()  # warm
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            one()
+        t = time.perf_counter() - t0
+        return {"value": world * steps * edges_per_step / 2 / t / 1e9, "unit": UNIT,
+                "h2d_bytes_per_step": 4 * (n + 1) + 4 * nnz + 4 * k,
+                "d2h_bytes_per_step": 12 * k * n,
+                "ms_per_step": 1e3 * t / steps,
+                "path": "tbfs_graph_create_csc (pinned host CSC) + tbfs_bfs_many (pinned host "
+                        "S/sigma) + tbfs_graph_destroy per step, host wall clock"}
+    finally:
+        for b in bufs:
+            L.tbfs_host_free_pinned(b)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_tbfs(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,132 @@
+/*
+ * tbfs.h -- native C ABI of the GB300 (sm_103a) linear-algebra BFS engine.
+ *
+ * The engine computes, for an unweighted graph held as a CSC adjacency
+ * (column v lists the in-neighbours u of v, i.e. edge u->v) and a root r:
+ *   S[v]     depth of v (root = 0, unreached = -1),
+ *   sigma[v] number of shortest paths r->v, counted with the multiplicity of
+ *            the CSC entries (int64; overflow past INT64_MAX is reported in
+ *            tbfs_stats.sigma_overflow instead of being rounded).
+ * These are the depth vector S and the path-count vector sigma of the
+ * reference's semiring BFS (TurboBFS_CSC_TD/bfstdcsc_seq.c:48-80 and
+ * TurboBFS_CSC_TD/spmvcsc_seq.c:22-41); both are unique functions of
+ * (graph, root), so every traversal direction returns identical values.
+ *
+ * The reference's own entry points (bfs_gpu_td_csc_sc and friends) are
+ * declared in tbfs_compat.h; the host graph tools in tbfs_graphgen.h.
+ *
+ * Threading: one tbfs_graph may be used by one host thread at a time.
+ * Every call returns a tbfs_status; nothing in the library calls exit().
+ */
+#ifndef TBFS_H
+#define TBFS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TBFS_VERSION 100
+
+typedef enum tbfs_status {
+  TBFS_OK = 0,
+  TBFS_ERR_INVALID_ARG = 1,   /* bad size, root out of range, null pointer  */
+  TBFS_ERR_CUDA = 2,          /* a CUDA runtime call failed                 */
+  TBFS_ERR_OUT_OF_MEMORY = 3, /* device or host allocation failed           */
+  TBFS_ERR_TIMEOUT = 4,       /* a grid barrier wait ran past its budget    */
+  TBFS_ERR_NO_DEVICE = 5,     /* no CUDA device visible                     */
+  TBFS_ERR_IO = 6,            /* file could not be read / parsed            */
+  TBFS_ERR_UNSUPPORTED = 7    /* valid request this build cannot serve      */
+} tbfs_status;
+
+typedef enum tbfs_mode {
+  TBFS_MODE_AUTO = 0,      /* direction-optimizing, switched on the device */
+  TBFS_MODE_TOP_DOWN = 1,  /* push from the frontier queue every level     */
+  TBFS_MODE_BOTTOM_UP = 2  /* pull into unvisited vertices every level     */
+} tbfs_mode;
+
+/* tbfs_graph_create_* flags */
+#define TBFS_GRAPH_SYMMETRIC 0x1u   /* caller guarantees in-lists == out-lists */
+#define TBFS_GRAPH_DEVICE_PTRS 0x2u /* input arrays are device pointers       */
+
+typedef struct tbfs_graph tbfs_graph;
+
+typedef struct tbfs_options {
+  int32_t mode;              /* tbfs_mode                                    */
+  int32_t want_sigma;        /* 0: S only; 1: S and sigma                    */
+  int32_t outputs_on_device; /* 1: S/sigma are device pointers               */
+  int32_t inject_barrier_skip; /* testing: k > 0 makes one CTA leave before
+                                  the barrier that ends level k-1, so the
+                                  others' bounded waits expire and the call
+                                  returns TBFS_ERR_TIMEOUT; 0 = off          */
+  float alpha;               /* TD->BU when frontier edges > unexplored/alpha */
+  float beta;                /* BU->TD when frontier size < n/beta           */
+  void *stream;              /* cudaStream_t; NULL = legacy default stream   */
+  int64_t timeout_ns;        /* grid-barrier wait budget; <=0 = 2 s          */
+} tbfs_options;
+
+typedef struct tbfs_stats {
+  int32_t levels;          /* non-empty BFS levels (max depth + 1)           */
+  int32_t td_levels;       /* levels expanded top-down                       */
+  int32_t bu_levels;       /* levels expanded bottom-up                      */
+  int32_t sigma_overflow;  /* 1 if some path count exceeded INT64_MAX         */
+  int64_t visited;         /* vertices reached, root included                */
+  int64_t edges;           /* sum of out-degrees of reached vertices         */
+  double device_ms;        /* CUDA-event time of the traversal on the stream */
+} tbfs_stats;
+
+/* Defaults: AUTO, want_sigma = 1, host outputs, alpha = 15, beta = 18. */
+void tbfs_options_init(tbfs_options *opt);
+
+/* Upload a CSC adjacency (col_ptr[n+1], row_idx[nnz], int32, 0-based).
+ * The graph stays resident until tbfs_graph_destroy.  Without
+ * TBFS_GRAPH_SYMMETRIC the transpose (out-lists) is built on the device. */
+tbfs_status tbfs_graph_create_csc(const int32_t *col_ptr, const int32_t *row_idx,
+                                  int32_t n, int64_t nnz, uint32_t flags,
+                                  tbfs_graph **out);
+
+/* Upload a COOC adjacency: entry k is the edge row[k] -> col[k] (the
+ * reference's ICOOC/JCOOC, TurboBFS_COOC_TD/bfstdcooc.h:29-32).  Column order
+ * is not required; the column pointer is rebuilt on the device. */
+tbfs_status tbfs_graph_create_cooc(const int32_t *row, const int32_t *col,
+                                   int32_t n, int64_t nnz, uint32_t flags,
+                                   tbfs_graph **out);
+
+void tbfs_graph_destroy(tbfs_graph *g);
+
+tbfs_status tbfs_graph_info(const tbfs_graph *g, int32_t *n, int64_t *nnz,
+                            uint32_t *flags);
+
+/* One BFS from root.  S must hold n int32; sigma n int64 (may be NULL when
+ * want_sigma = 0).  stats may be NULL.  Synchronous unless outputs are on
+ * the device, in which case it returns after enqueueing on opt->stream;
+ * stats->device_ms is then filled by tbfs_graph_last_stats after a sync. */
+tbfs_status tbfs_bfs(tbfs_graph *g, int32_t root, const tbfs_options *opt,
+                     int32_t *S, int64_t *sigma, tbfs_stats *stats);
+
+/* Statistics of the most recent traversal on g (synchronizes its stream). */
+tbfs_status tbfs_graph_last_stats(tbfs_graph *g, tbfs_stats *stats);
+
+/* k BFS runs, one per root, back to back on one stream.  Row i of the
+ * outputs (stride n) receives root i's result; stats[i] likewise. */
+tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_t k,
+                          const tbfs_options *opt, int32_t *S, int64_t *sigma,
+                          tbfs_stats *stats);
+
+/* Page-locked host buffers for fast host<->device copies. */
+tbfs_status tbfs_host_alloc_pinned(size_t bytes, void **ptr);
+void tbfs_host_free_pinned(void *ptr);
+
+const char *tbfs_status_string(tbfs_status s);
+/* Detail of the last failure on the calling thread ("" if none). */
+const char *tbfs_last_error(void);
+int32_t tbfs_version(void);
+/* Number of visible CUDA devices (0 on a machine without a GPU). */
+int32_t tbfs_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TBFS_H */

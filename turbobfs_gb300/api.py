@@ -1,0 +1,212 @@
+"""Python face of the engine.
+
+Two layers, both thin wrappers over the C ABI:
+
+* ``Graph`` -- a device-resident graph (``tbfs_graph_create_*``) with
+  ``bfs`` / ``bfs_many`` returning numpy depth (int32, -1 unreached) and
+  path-count (int64) vectors plus traversal statistics.
+* ``bfs_gpu_td_csc_sc`` ... ``bfs_gpu_td_cooc_sc`` -- the reference's entry
+  points under their own names and argument order
+  (TurboBFS_CSC_TD/bfstdcsc.h:54-66, TurboBFS_CSC_BU/bfsbucsc.h:55-67,
+  TurboBFS_CSC_TDBU/bfstdbucsc.h:56-68, TurboBFS_COOC_TD/bfstdcooc.h:48-49):
+  host arrays in, results written into the caller's arrays, int status out.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import GRAPH_SYMMETRIC, Options, Stats, check, lib
+
+MODES = {"auto": 0, "do": 0, "td": 1, "top_down": 1, "bu": 2, "bottom_up": 2}
+_P_I32 = ctypes.POINTER(ctypes.c_int32)
+_P_I64 = ctypes.POINTER(ctypes.c_int64)
+_P_F32 = ctypes.POINTER(ctypes.c_float)
+
+
+def _i32(a) -> np.ndarray:
+    a = np.asarray(a)
+    if a.dtype != np.int32 or not a.flags.c_contiguous:
+        a = np.ascontiguousarray(a, dtype=np.int32)
+    return a
+
+
+def _ptr(a: np.ndarray, typ):
+    return a.ctypes.data_as(typ)
+
+
+def make_options(mode="auto", sigma=True, alpha=None, beta=None, timeout_ns=0,
+                 outputs_on_device=False, stream=None, inject_barrier_skip=0) -> Options:
+    o = Options()
+    lib().tbfs_options_init(ctypes.byref(o))
+    o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
+    o.want_sigma = 1 if sigma else 0
+    o.outputs_on_device = 1 if outputs_on_device else 0
+    if alpha is not None:
+        o.alpha = float(alpha)
+    if beta is not None:
+        o.beta = float(beta)
+    o.timeout_ns = int(timeout_ns)
+    o.stream = stream
+    o.inject_barrier_skip = int(inject_barrier_skip)
+    return o
+
+
+@dataclass
+class BfsResult:
+    S: np.ndarray                 # int32[n], -1 = unreached
+    sigma: np.ndarray | None      # int64[n] path counts (None if not requested)
+    stats: dict = field(default_factory=dict)
+
+
+class Graph:
+    """A graph resident in GPU memory until ``close()``."""
+
+    def __init__(self, col_ptr, row_idx, n: int | None = None, symmetric: bool = False):
+        cp, ic = _i32(col_ptr), _i32(row_idx)
+        self.n = int(n if n is not None else cp.shape[0] - 1)
+        self.nnz = int(ic.shape[0])
+        self.symmetric = bool(symmetric)
+        h = ctypes.c_void_p()
+        check(lib().tbfs_graph_create_csc(_ptr(cp, _P_I32), _ptr(ic, _P_I32), self.n, self.nnz,
+                                          GRAPH_SYMMETRIC if symmetric else 0, ctypes.byref(h)),
+              "tbfs_graph_create_csc")
+        self._h = h
+
+    @classmethod
+    def from_host_csc(cls, g) -> "Graph":
+        return cls(g.col_ptr, g.row_idx, g.n, symmetric=g.symmetric)
+
+    @classmethod
+    def from_cooc(cls, I, J, n: int, symmetric: bool = False) -> "Graph":
+        I, J = _i32(I), _i32(J)
+        self = cls.__new__(cls)
+        self.n, self.nnz, self.symmetric = int(n), int(I.shape[0]), bool(symmetric)
+        h = ctypes.c_void_p()
+        check(lib().tbfs_graph_create_cooc(_ptr(I, _P_I32), _ptr(J, _P_I32), self.n, self.nnz,
+                                           GRAPH_SYMMETRIC if symmetric else 0, ctypes.byref(h)),
+              "tbfs_graph_create_cooc")
+        self._h = h
+        return self
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        if self._h is None:
+            raise RuntimeError("graph is closed")
+        return self._h
+
+    def bfs(self, root: int, mode="auto", sigma: bool = True, **kw) -> BfsResult:
+        o = make_options(mode, sigma, **kw)
+        S = np.empty(self.n, dtype=np.int32)
+        sg = np.empty(self.n, dtype=np.int64) if sigma else None
+        st = Stats()
+        check(lib().tbfs_bfs(self.handle, int(root), ctypes.byref(o), _ptr(S, _P_I32),
+                             _ptr(sg, _P_I64) if sg is not None else None, ctypes.byref(st)),
+              "tbfs_bfs")
+        return BfsResult(S, sg, st.as_dict())
+
+    def bfs_many(self, roots, mode="auto", sigma: bool = True, **kw):
+        roots = _i32(roots)
+        k = int(roots.shape[0])
+        o = make_options(mode, sigma, **kw)
+        S = np.empty((k, self.n), dtype=np.int32)
+        sg = np.empty((k, self.n), dtype=np.int64) if sigma else None
+        stats = (Stats * max(k, 1))()
+        check(lib().tbfs_bfs_many(self.handle, _ptr(roots, _P_I32), k, ctypes.byref(o),
+                                  _ptr(S, _P_I32), _ptr(sg, _P_I64) if sg is not None else None,
+                                  stats), "tbfs_bfs_many")
+        return S, sg, [stats[i].as_dict() for i in range(k)]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().tbfs_graph_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- compat ---
+# Same names, argument order and in-place outputs as the reference's C
+# functions; the int return is 0 on success, a tbfs_status code otherwise.
+
+def _outbuf(a, dtype, n: int, name: str) -> np.ndarray:
+    if not (isinstance(a, np.ndarray) and a.dtype == dtype and a.flags.c_contiguous
+            and a.shape[0] >= n):
+        raise TypeError(f"{name} must be a contiguous {np.dtype(dtype).name} array of length >= n")
+    return a
+
+
+def bfs_gpu_td_csc_sc(IC_h, CP_h, S_h, sigma_h, r, nz, n, repetition=1) -> int:
+    IC, CP = _i32(IC_h), _i32(CP_h)
+    S, sg = _outbuf(S_h, np.int32, n, "S_h"), _outbuf(sigma_h, np.float32, n, "sigma_h")
+    return lib().bfs_gpu_td_csc_sc(_ptr(IC, _P_I32), _ptr(CP, _P_I32), _ptr(S, _P_I32),
+                                   _ptr(sg, _P_F32), r, nz, n, repetition)
+
+
+def bfs_gpu_td_csc_wa(IC_h, CP_h, S_h, sigma_h, r, nz, n, repetition=1) -> int:
+    IC, CP = _i32(IC_h), _i32(CP_h)
+    S, sg = _outbuf(S_h, np.int32, n, "S_h"), _outbuf(sigma_h, np.float32, n, "sigma_h")
+    return lib().bfs_gpu_td_csc_wa(_ptr(IC, _P_I32), _ptr(CP, _P_I32), _ptr(S, _P_I32),
+                                   _ptr(sg, _P_F32), r, nz, n, repetition)
+
+
+def bfs_gpu_bu_csc_sc(I_h, CP_h, S_h, r, nz, n, repetition=1, bbreak=1) -> int:
+    I, CP = _i32(I_h), _i32(CP_h)
+    S = _outbuf(S_h, np.int32, n, "S_h")
+    return lib().bfs_gpu_bu_csc_sc(_ptr(I, _P_I32), _ptr(CP, _P_I32), _ptr(S, _P_I32), r, nz, n,
+                                   repetition, bbreak)
+
+
+def bfs_gpu_bu_csc_wa(I_h, CP_h, S_h, r, nz, n, repetition=1, bbreak=1) -> int:
+    I, CP = _i32(I_h), _i32(CP_h)
+    S = _outbuf(S_h, np.int32, n, "S_h")
+    return lib().bfs_gpu_bu_csc_wa(_ptr(I, _P_I32), _ptr(CP, _P_I32), _ptr(S, _P_I32), r, nz, n,
+                                   repetition, bbreak)
+
+
+def bfs_gpu_tdbu_csc_sc(I_h, CP_h, S_h, sigma_h, r, nz, n, repetition=1, bbreak=1) -> int:
+    I, CP = _i32(I_h), _i32(CP_h)
+    S, sg = _outbuf(S_h, np.int32, n, "S_h"), _outbuf(sigma_h, np.int32, n, "sigma_h")
+    return lib().bfs_gpu_tdbu_csc_sc(_ptr(I, _P_I32), _ptr(CP, _P_I32), _ptr(S, _P_I32),
+                                     _ptr(sg, _P_I32), r, nz, n, repetition, bbreak)
+
+
+def bfs_gpu_tdbu_csc_wa(IC_h, CP_h, S_h, sigma_h, r, nz, n, repetition=1, bbreak=1) -> int:
+    IC, CP = _i32(IC_h), _i32(CP_h)
+    S, sg = _outbuf(S_h, np.int32, n, "S_h"), _outbuf(sigma_h, np.int32, n, "sigma_h")
+    return lib().bfs_gpu_tdbu_csc_wa(_ptr(IC, _P_I32), _ptr(CP, _P_I32), _ptr(S, _P_I32),
+                                     _ptr(sg, _P_I32), r, nz, n, repetition, bbreak)
+
+
+def bfs_gpu_td_cooc_sc(I_h, J_h, sigma_h, r, nz, n, repetition=1) -> int:
+    I, J = _i32(I_h), _i32(J_h)
+    sg = _outbuf(sigma_h, np.float32, n, "sigma_h")
+    return lib().bfs_gpu_td_cooc_sc(_ptr(I, _P_I32), _ptr(J, _P_I32), _ptr(sg, _P_F32), r, nz,
+                                    n, repetition)
+
+
+COMPAT_FUNCTIONS = {
+    "bfs_gpu_td_csc_sc": bfs_gpu_td_csc_sc,
+    "bfs_gpu_td_csc_wa": bfs_gpu_td_csc_wa,
+    "bfs_gpu_bu_csc_sc": bfs_gpu_bu_csc_sc,
+    "bfs_gpu_bu_csc_wa": bfs_gpu_bu_csc_wa,
+    "bfs_gpu_tdbu_csc_sc": bfs_gpu_tdbu_csc_sc,
+    "bfs_gpu_tdbu_csc_wa": bfs_gpu_tdbu_csc_wa,
+    "bfs_gpu_td_cooc_sc": bfs_gpu_td_cooc_sc,
+}
+
+
+def device_count() -> int:
+    return int(lib().tbfs_device_count())

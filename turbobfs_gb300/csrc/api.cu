@@ -1,0 +1,623 @@
+/*
+ * api.cu -- the C ABI: resident graphs, single and repeated traversals, and
+ * the drop-in replacements for the reference's GPU entry points.
+ */
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "tbfs.h"
+#include "tbfs_compat.h"
+#include "tbfs_internal.h"
+
+using tbfs::BfsCtl;
+using tbfs::BfsParams;
+
+/* ------------------------------------------------------------- errors */
+
+static thread_local char g_err[512];
+
+extern "C" void tbfs_set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+extern "C" const char *tbfs_last_error(void) { return g_err; }
+
+static tbfs_status cuda_fail(cudaError_t e, const char *what, int line) {
+  tbfs_set_error("%s: %s (api.cu:%d)", what, cudaGetErrorString(e), line);
+  return e == cudaErrorMemoryAllocation ? TBFS_ERR_OUT_OF_MEMORY : TBFS_ERR_CUDA;
+}
+
+#define CUDA_TRY(call)                                          \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call, __LINE__); \
+  } while (0)
+
+static tbfs_status invalid(const char *msg) {
+  tbfs_set_error("%s", msg);
+  return TBFS_ERR_INVALID_ARG;
+}
+
+extern "C" const char *tbfs_status_string(tbfs_status s) {
+  switch (s) {
+    case TBFS_OK: return "ok";
+    case TBFS_ERR_INVALID_ARG: return "invalid argument";
+    case TBFS_ERR_CUDA: return "CUDA error";
+    case TBFS_ERR_OUT_OF_MEMORY: return "out of memory";
+    case TBFS_ERR_TIMEOUT: return "grid barrier timeout";
+    case TBFS_ERR_NO_DEVICE: return "no CUDA device";
+    case TBFS_ERR_IO: return "I/O error";
+    case TBFS_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+extern "C" int32_t tbfs_version(void) { return TBFS_VERSION; }
+
+extern "C" int32_t tbfs_device_count(void) {
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return c;
+}
+
+extern "C" void tbfs_options_init(tbfs_options *opt) {
+  if (!opt) return;
+  memset(opt, 0, sizeof(*opt));
+  opt->mode = TBFS_MODE_AUTO;
+  opt->want_sigma = 1;
+  opt->alpha = 15.0f;
+  opt->beta = 18.0f;
+}
+
+extern "C" tbfs_status tbfs_host_alloc_pinned(size_t bytes, void **ptr) {
+  if (!ptr) return invalid("tbfs_host_alloc_pinned: null out pointer");
+  *ptr = nullptr;
+  CUDA_TRY(cudaMallocHost(ptr, bytes ? bytes : 1));
+  return TBFS_OK;
+}
+
+extern "C" void tbfs_host_free_pinned(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+
+/* ------------------------------------------------------------- graphs */
+
+static void graph_free(tbfs_graph *g) {
+  if (!g) return;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(g->device);
+  if (g->separate_out) {
+    cudaFree(g->rp);
+    cudaFree(g->jr);
+  }
+  cudaFree(g->cp);
+  cudaFree(g->ic);
+  cudaFree(g->q0);
+  cudaFree(g->q1);
+  cudaFree(g->e0);
+  cudaFree(g->e1);
+  cudaFree(g->ctl);
+  cudaFree(g->S_dev);
+  cudaFree(g->sigma_dev);
+  if (g->ctl_host) cudaFreeHost(g->ctl_host);
+  if (g->ev0) cudaEventDestroy(g->ev0);
+  if (g->ev1) cudaEventDestroy(g->ev1);
+  cudaSetDevice(cur);
+  delete g;
+}
+
+extern "C" void tbfs_graph_destroy(tbfs_graph *g) { graph_free(g); }
+
+static tbfs_status need_device() {
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (e != cudaSuccess || c == 0) {
+    cudaGetLastError();
+    tbfs_set_error("no CUDA device visible");
+    return TBFS_ERR_NO_DEVICE;
+  }
+  return TBFS_OK;
+}
+
+/* allocations shared by both constructors, after cp/ic/rp/jr are set */
+static tbfs_status graph_finish(tbfs_graph *g) {
+  const size_t n = (size_t)g->n;
+  CUDA_TRY(cudaMalloc(&g->q0, n * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->q1, n * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->e0, n * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->e1, n * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->ctl, sizeof(BfsCtl)));
+  CUDA_TRY(cudaMallocHost(&g->ctl_host, sizeof(BfsCtl)));
+  memset(g->ctl_host, 0, sizeof(BfsCtl));
+  CUDA_TRY(cudaEventCreate(&g->ev0));
+  CUDA_TRY(cudaEventCreate(&g->ev1));
+  CUDA_TRY(tbfs::bfs_geometry(g->device, &g->geom));
+  g->out_edges_total = g->nnz;
+  return TBFS_OK;
+}
+
+static tbfs_status read_flag(const int *d_flag, cudaStream_t s, int *flag) {
+  CUDA_TRY(cudaMemcpyAsync(flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return TBFS_OK;
+}
+
+static tbfs_status build_csc(tbfs_graph *g, const int32_t *col_ptr, const int32_t *row_idx,
+                             int *d_flag) {
+  const size_t n = (size_t)g->n, nnz = (size_t)g->nnz;
+  const cudaMemcpyKind kind = (g->flags & TBFS_GRAPH_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice
+                                                                  : cudaMemcpyHostToDevice;
+  CUDA_TRY(cudaMalloc(&g->cp, (n + 1) * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->ic, (nnz ? nnz : 1) * sizeof(int)));
+  CUDA_TRY(cudaMemcpy(g->cp, col_ptr, (n + 1) * sizeof(int), kind));
+  if (nnz) CUDA_TRY(cudaMemcpy(g->ic, row_idx, nnz * sizeof(int), kind));
+  CUDA_TRY(cudaMemset(d_flag, 0, sizeof(int)));
+  CUDA_TRY(tbfs::validate_csc(g->cp, g->ic, g->n, g->nnz, d_flag, 0));
+  int flag = 0;
+  tbfs_status st = read_flag(d_flag, 0, &flag);
+  if (st != TBFS_OK) return st;
+  if (flag & 1) return invalid("col_ptr must start at 0, be nondecreasing and end at nnz");
+  if (flag & 2) return invalid("row index outside [0, n)");
+  if (g->flags & TBFS_GRAPH_SYMMETRIC) {
+    g->rp = g->cp;
+    g->jr = g->ic;
+    return TBFS_OK;
+  }
+  /* out-lists = transpose: key = row id, value = column id */
+  int *col = nullptr;
+  CUDA_TRY(cudaMalloc(&col, (nnz ? nnz : 1) * sizeof(int)));
+  g->separate_out = true;
+  cudaError_t e = cudaMalloc(&g->rp, (n + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&g->jr, (nnz ? nnz : 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::expand_columns(g->cp, g->n, col, 0);
+  if (e == cudaSuccess)
+    e = tbfs::counting_sort_lists(g->ic, col, g->nnz, g->n, g->rp, g->jr, d_flag, 0);
+  cudaFree(col);
+  if (e != cudaSuccess) return cuda_fail(e, "transpose", __LINE__);
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_graph_create_csc(const int32_t *col_ptr, const int32_t *row_idx,
+                                             int32_t n, int64_t nnz, uint32_t flags,
+                                             tbfs_graph **out) {
+  if (!out) return invalid("tbfs_graph_create_csc: null out pointer");
+  *out = nullptr;
+  if (n < 1 || nnz < 0 || nnz > INT32_MAX || !col_ptr || (nnz > 0 && !row_idx))
+    return invalid("tbfs_graph_create_csc: need n >= 1, 0 <= nnz <= INT32_MAX, arrays");
+  tbfs_status st = need_device();
+  if (st != TBFS_OK) return st;
+  tbfs_graph *g = new tbfs_graph();
+  cudaGetDevice(&g->device);
+  g->n = n;
+  g->nnz = nnz;
+  g->flags = flags;
+  int *d_flag = nullptr;
+  cudaError_t e = cudaMalloc(&d_flag, sizeof(int));
+  if (e != cudaSuccess) {
+    graph_free(g);
+    return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
+  }
+  st = build_csc(g, col_ptr, row_idx, d_flag);
+  cudaFree(d_flag);
+  if (st == TBFS_OK) st = graph_finish(g);
+  if (st != TBFS_OK) {
+    graph_free(g);
+    return st;
+  }
+  *out = g;
+  return TBFS_OK;
+}
+
+static tbfs_status build_cooc(tbfs_graph *g, const int32_t *row, const int32_t *col,
+                              int *d_flag) {
+  const size_t n = (size_t)g->n, nnz = (size_t)g->nnz;
+  const cudaMemcpyKind kind = (g->flags & TBFS_GRAPH_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice
+                                                                  : cudaMemcpyHostToDevice;
+  int *dr = nullptr, *dc = nullptr;
+  cudaError_t e = cudaMalloc(&dr, (nnz ? nnz : 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&dc, (nnz ? nnz : 1) * sizeof(int));
+  if (e == cudaSuccess && nnz) e = cudaMemcpy(dr, row, nnz * sizeof(int), kind);
+  if (e == cudaSuccess && nnz) e = cudaMemcpy(dc, col, nnz * sizeof(int), kind);
+  if (e == cudaSuccess) e = cudaMemset(d_flag, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&g->cp, (n + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&g->ic, (nnz ? nnz : 1) * sizeof(int));
+  /* in-lists: key = column (target), value = row (source) */
+  if (e == cudaSuccess)
+    e = tbfs::counting_sort_lists(dc, dr, g->nnz, g->n, g->cp, g->ic, d_flag, 0);
+  if (e == cudaSuccess && !(g->flags & TBFS_GRAPH_SYMMETRIC)) {
+    g->separate_out = true;
+    e = cudaMalloc(&g->rp, (n + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&g->jr, (nnz ? nnz : 1) * sizeof(int));
+    if (e == cudaSuccess)
+      e = tbfs::counting_sort_lists(dr, dc, g->nnz, g->n, g->rp, g->jr, d_flag, 0);
+  } else if (e == cudaSuccess) {
+    g->rp = g->cp;
+    g->jr = g->ic;
+  }
+  cudaFree(dr);
+  cudaFree(dc);
+  if (e != cudaSuccess) return cuda_fail(e, "COOC ingest", __LINE__);
+  int flag = 0;
+  tbfs_status st = read_flag(d_flag, 0, &flag);
+  if (st != TBFS_OK) return st;
+  if (flag) return invalid("COOC entry outside [0, n)");
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_graph_create_cooc(const int32_t *row, const int32_t *col,
+                                              int32_t n, int64_t nnz, uint32_t flags,
+                                              tbfs_graph **out) {
+  if (!out) return invalid("tbfs_graph_create_cooc: null out pointer");
+  *out = nullptr;
+  if (n < 1 || nnz < 0 || nnz > INT32_MAX || (nnz > 0 && (!row || !col)))
+    return invalid("tbfs_graph_create_cooc: need n >= 1, 0 <= nnz <= INT32_MAX, arrays");
+  tbfs_status st = need_device();
+  if (st != TBFS_OK) return st;
+  tbfs_graph *g = new tbfs_graph();
+  cudaGetDevice(&g->device);
+  g->n = n;
+  g->nnz = nnz;
+  g->flags = flags;
+  int *d_flag = nullptr;
+  cudaError_t e = cudaMalloc(&d_flag, sizeof(int));
+  if (e != cudaSuccess) {
+    graph_free(g);
+    return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
+  }
+  st = build_cooc(g, row, col, d_flag);
+  cudaFree(d_flag);
+  if (st == TBFS_OK) st = graph_finish(g);
+  if (st != TBFS_OK) {
+    graph_free(g);
+    return st;
+  }
+  *out = g;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_graph_info(const tbfs_graph *g, int32_t *n, int64_t *nnz,
+                                       uint32_t *flags) {
+  if (!g) return invalid("tbfs_graph_info: null graph");
+  if (n) *n = g->n;
+  if (nnz) *nnz = g->nnz;
+  if (flags) *flags = g->flags;
+  return TBFS_OK;
+}
+
+/* --------------------------------------------------------- traversal */
+
+static tbfs_status check_opts(const tbfs_graph *g, int32_t root, const tbfs_options &o,
+                              const int32_t *S, const int64_t *sigma) {
+  if (!g) return invalid("null graph");
+  if (root < 0 || root >= g->n) return invalid("root outside [0, n)");
+  if (!S) return invalid("null S output");
+  if (o.want_sigma && !sigma) return invalid("want_sigma set but sigma output is null");
+  if (o.mode < TBFS_MODE_AUTO || o.mode > TBFS_MODE_BOTTOM_UP) return invalid("bad mode");
+  if (!(o.alpha > 0.0f) || !(o.beta > 0.0f)) return invalid("alpha and beta must be > 0");
+  return TBFS_OK;
+}
+
+static tbfs_options resolve_opts(const tbfs_options *in) {
+  tbfs_options o;
+  tbfs_options_init(&o);
+  if (in) o = *in;
+  if (o.alpha <= 0.0f) o.alpha = 15.0f;
+  if (o.beta <= 0.0f) o.beta = 18.0f;
+  return o;
+}
+
+static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o, int *S,
+                             unsigned long long *sigma) {
+  BfsParams p;
+  p.cp = g->cp;
+  p.ic = g->ic;
+  p.rp = g->rp;
+  p.jr = g->jr;
+  p.S = S;
+  p.sigma = o.want_sigma ? sigma : nullptr;
+  p.q0 = g->q0;
+  p.q1 = g->q1;
+  p.e0 = g->e0;
+  p.e1 = g->e1;
+  p.ctl = g->ctl;
+  p.out_edges_total = g->out_edges_total;
+  p.timeout_ns = o.timeout_ns > 0 ? o.timeout_ns : 2000000000LL;
+  p.n = g->n;
+  p.root = root;
+  p.mode = o.mode;
+  p.symmetric = g->separate_out ? 0 : 1;
+  p.alpha = o.alpha;
+  p.beta = o.beta;
+  p.inject_barrier_skip = o.inject_barrier_skip > 0 ? o.inject_barrier_skip : 0;
+  return p;
+}
+
+/* enqueue: clear control block, time and launch, copy control block back */
+static tbfs_status enqueue_bfs(tbfs_graph *g, const BfsParams &p, cudaStream_t s,
+                               cudaEvent_t ev0, cudaEvent_t ev1, BfsCtl *ctl_host) {
+  CUDA_TRY(cudaMemsetAsync(g->ctl, 0, sizeof(BfsCtl), s));
+  CUDA_TRY(cudaEventRecord(ev0, s));
+  CUDA_TRY(tbfs::bfs_launch(p, g->geom, s));
+  CUDA_TRY(cudaEventRecord(ev1, s));
+  CUDA_TRY(cudaMemcpyAsync(ctl_host, g->ctl, sizeof(BfsCtl), cudaMemcpyDeviceToHost, s));
+  return TBFS_OK;
+}
+
+static tbfs_status stats_from(const BfsCtl &c, cudaEvent_t ev0, cudaEvent_t ev1,
+                              tbfs_stats *st) {
+  float ms = 0.0f;
+  cudaError_t e = cudaEventElapsedTime(&ms, ev0, ev1);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime", __LINE__);
+  st->levels = c.levels;
+  st->td_levels = c.td_levels;
+  st->bu_levels = c.bu_levels;
+  st->sigma_overflow = c.sigma_overflow;
+  st->visited = c.visited;
+  st->edges = c.edges;
+  st->device_ms = ms;
+  if (c.status != 0) {
+    tbfs_set_error("traversal stopped: grid barrier wait exceeded its budget at level %d",
+                   c.timeout_level - 2);
+    return TBFS_ERR_TIMEOUT;
+  }
+  return TBFS_OK;
+}
+
+static tbfs_status ensure_result_buffers(tbfs_graph *g, bool sigma) {
+  if (!g->S_dev) CUDA_TRY(cudaMalloc(&g->S_dev, (size_t)g->n * sizeof(int)));
+  if (sigma && !g->sigma_dev)
+    CUDA_TRY(cudaMalloc(&g->sigma_dev, (size_t)g->n * sizeof(unsigned long long)));
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_graph_last_stats(tbfs_graph *g, tbfs_stats *stats) {
+  if (!g || !stats) return invalid("tbfs_graph_last_stats: null argument");
+  CUDA_TRY(cudaSetDevice(g->device));
+  if (g->pending) {
+    CUDA_TRY(cudaStreamSynchronize(g->last_stream));
+    g->pending = false;
+    tbfs_stats st = {};
+    tbfs_status s = stats_from(*g->ctl_host, g->ev0, g->ev1, &st);
+    g->last = st;
+    if (s != TBFS_OK) {
+      *stats = st;
+      return s;
+    }
+  }
+  *stats = g->last;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_bfs(tbfs_graph *g, int32_t root, const tbfs_options *opt,
+                                int32_t *S, int64_t *sigma, tbfs_stats *stats) {
+  const tbfs_options o = resolve_opts(opt);
+  tbfs_status st = check_opts(g, root, o, S, sigma);
+  if (st != TBFS_OK) return st;
+  CUDA_TRY(cudaSetDevice(g->device));
+  cudaStream_t s = (cudaStream_t)o.stream;
+  int *S_dst = S;
+  unsigned long long *sig_dst = reinterpret_cast<unsigned long long *>(sigma);
+  if (!o.outputs_on_device) {
+    if ((st = ensure_result_buffers(g, o.want_sigma != 0)) != TBFS_OK) return st;
+    S_dst = g->S_dev;
+    sig_dst = g->sigma_dev;
+  }
+  const BfsParams p = make_params(g, root, o, S_dst, sig_dst);
+  if ((st = enqueue_bfs(g, p, s, g->ev0, g->ev1, g->ctl_host)) != TBFS_OK) return st;
+  g->pending = true;
+  g->last_stream = s;
+  if (!o.outputs_on_device) {
+    CUDA_TRY(cudaMemcpyAsync(S, S_dst, (size_t)g->n * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (o.want_sigma)
+      CUDA_TRY(cudaMemcpyAsync(sigma, sig_dst, (size_t)g->n * sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, s));
+  }
+  if (stats || !o.outputs_on_device) {
+    tbfs_stats tmp = {};
+    st = tbfs_graph_last_stats(g, &tmp);
+    if (stats) *stats = tmp;
+    return st;
+  }
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_t k,
+                                     const tbfs_options *opt, int32_t *S, int64_t *sigma,
+                                     tbfs_stats *stats) {
+  const tbfs_options o = resolve_opts(opt);
+  if (!g || !roots || k < 0) return invalid("tbfs_bfs_many: bad arguments");
+  if (k == 0) return TBFS_OK;
+  for (int32_t i = 0; i < k; ++i) {
+    tbfs_status st = check_opts(g, roots[i], o, S, sigma);
+    if (st != TBFS_OK) return st;
+  }
+  CUDA_TRY(cudaSetDevice(g->device));
+  cudaStream_t s = (cudaStream_t)o.stream;
+  tbfs_status st = TBFS_OK;
+  if (!o.outputs_on_device && (st = ensure_result_buffers(g, o.want_sigma != 0)) != TBFS_OK)
+    return st;
+  std::vector<cudaEvent_t> ev(2 * (size_t)k, nullptr);
+  BfsCtl *ctl_h = nullptr;
+  cudaError_t e = cudaMallocHost(&ctl_h, (size_t)k * sizeof(BfsCtl));
+  for (size_t i = 0; e == cudaSuccess && i < ev.size(); ++i) e = cudaEventCreate(&ev[i]);
+  const size_t n = (size_t)g->n;
+  for (int32_t i = 0; e == cudaSuccess && st == TBFS_OK && i < k; ++i) {
+    int *S_dst = o.outputs_on_device ? S + i * n : g->S_dev;
+    unsigned long long *sig_dst =
+        o.outputs_on_device ? reinterpret_cast<unsigned long long *>(sigma) + (o.want_sigma ? i * n : 0)
+                            : g->sigma_dev;
+    const BfsParams p = make_params(g, roots[i], o, S_dst, sig_dst);
+    st = enqueue_bfs(g, p, s, ev[2 * i], ev[2 * i + 1], ctl_h + i);
+    if (st == TBFS_OK && !o.outputs_on_device) {
+      e = cudaMemcpyAsync(S + i * n, S_dst, n * sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess && o.want_sigma)
+        e = cudaMemcpyAsync(sigma + i * n, sig_dst, n * sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s);
+    }
+  }
+  if (e == cudaSuccess && st == TBFS_OK) e = cudaStreamSynchronize(s);
+  for (int32_t i = 0; e == cudaSuccess && st == TBFS_OK && i < k; ++i) {
+    tbfs_stats tmp = {};
+    st = stats_from(ctl_h[i], ev[2 * i], ev[2 * i + 1], &tmp);
+    if (stats) stats[i] = tmp;
+    g->last = tmp;
+  }
+  for (auto x : ev)
+    if (x) cudaEventDestroy(x);
+  if (ctl_h) cudaFreeHost(ctl_h);
+  g->pending = false;
+  if (e != cudaSuccess) return cuda_fail(e, "tbfs_bfs_many", __LINE__);
+  return st;
+}
+
+/* ------------------------------------------------------- compat shims */
+
+namespace {
+
+struct CompatRun {
+  std::vector<int32_t> S;
+  std::vector<int64_t> sigma;
+  tbfs_stats st = {};
+  double total_ms = 0.0;
+  int reps = 0;
+};
+
+/* Upload (CSC or COOC), run `repetition` traversals, keep the last result.
+ * The graph is treated as general (directed): the caller's arrays carry no
+ * symmetry promise. */
+int compat_run(const int *a, const int *b, bool cooc, int r, int nz, int n, int repetition,
+               bool want_sigma, CompatRun &out) {
+  if (n < 1 || nz < 0 || r < 0 || r >= n || (nz > 0 && (!a || !b)) || (!cooc && !b)) {
+    tbfs_set_error("invalid arguments: n=%d nz=%d r=%d", n, nz, r);
+    return TBFS_ERR_INVALID_ARG;
+  }
+  tbfs_graph *g = nullptr;
+  tbfs_status st = cooc ? tbfs_graph_create_cooc(a, b, n, nz, 0u, &g)
+                        : tbfs_graph_create_csc(b, a, n, nz, 0u, &g);
+  if (st != TBFS_OK) return st;
+  tbfs_options o;
+  tbfs_options_init(&o);
+  o.want_sigma = want_sigma ? 1 : 0;
+  out.S.assign((size_t)n, 0);
+  if (want_sigma) out.sigma.assign((size_t)n, 0);
+  out.reps = repetition < 1 ? 1 : repetition;
+  for (int i = 0; i < out.reps && st == TBFS_OK; ++i) {
+    st = tbfs_bfs(g, r, &o, out.S.data(), want_sigma ? out.sigma.data() : nullptr, &out.st);
+    out.total_ms += out.st.device_ms;
+  }
+  tbfs_graph_destroy(g);
+  if (st == TBFS_OK && getenv("TBFS_PRINT_TIMES"))
+    printf("tbfs: levels = %d, r = %d, average time BFS = %lfms\n", out.st.levels, r,
+           out.total_ms / out.reps);
+  return st;
+}
+
+void to_td_outputs(const CompatRun &run, int n, int *S_h, float *sigma_h) {
+  for (int v = 0; v < n; ++v) {
+    S_h[v] = run.S[v] < 0 ? 0 : run.S[v];
+    if (sigma_h) sigma_h[v] = (float)run.sigma[v];
+  }
+}
+
+int td_csc(int *IC_h, int *CP_h, int *S_h, float *sigma_h, int r, int nz, int n, int rep) {
+  if (!S_h || !sigma_h) return TBFS_ERR_INVALID_ARG;
+  CompatRun run;
+  int st = compat_run(IC_h, CP_h, false, r, nz, n, rep, true, run);
+  if (st == TBFS_OK) to_td_outputs(run, n, S_h, sigma_h);
+  return st;
+}
+
+int bu_csc(int *I_h, int *CP_h, int *S_h, int r, int nz, int n, int rep) {
+  if (!S_h) return TBFS_ERR_INVALID_ARG;
+  CompatRun run;
+  int st = compat_run(I_h, CP_h, false, r, nz, n, rep, false, run);
+  if (st == TBFS_OK) memcpy(S_h, run.S.data(), (size_t)n * sizeof(int));
+  return st;
+}
+
+/* The reference's TDBU drivers keep sigma only for the levels they expand
+ * top-down: they stay top-down while the last level held at most
+ * 0.001f*n vertices (a float compare, bfsgputdbucsc_sc.cu:112-122) and
+ * never switch back, and their bottom-up kernel leaves sigma at 0. */
+int tdbu_csc(int *I_h, int *CP_h, int *S_h, int *sigma_h, int r, int nz, int n, int rep) {
+  if (!S_h || !sigma_h) return TBFS_ERR_INVALID_ARG;
+  CompatRun run;
+  int st = compat_run(I_h, CP_h, false, r, nz, n, rep, true, run);
+  if (st != TBFS_OK) return st;
+  std::vector<int64_t> cnt((size_t)run.st.levels + 1, 0);
+  for (int v = 0; v < n; ++v)
+    if (run.S[v] >= 0 && run.S[v] < (int)cnt.size()) cnt[run.S[v]]++;
+  const float thr_td = 0.001f;
+  const float thresh_td = thr_td * (float)n;
+  int last_td = run.st.levels; /* deepest level reached top-down */
+  for (int d = 1; d < run.st.levels; ++d)
+    if ((float)cnt[d] > thresh_td) {
+      last_td = d;
+      break;
+    }
+  for (int v = 0; v < n; ++v) {
+    S_h[v] = run.S[v];
+    const bool td_level = run.S[v] >= 0 && run.S[v] <= last_td;
+    sigma_h[v] = td_level ? (int32_t)(uint32_t)(uint64_t)run.sigma[v] : 0;
+  }
+  return TBFS_OK;
+}
+
+}  // namespace
+
+extern "C" int bfs_gpu_td_csc_sc(int *IC_h, int *CP_h, int *S_h, float *sigma_h, int r,
+                                 int nz, int n, int repetition) {
+  return td_csc(IC_h, CP_h, S_h, sigma_h, r, nz, n, repetition);
+}
+
+extern "C" int bfs_gpu_td_csc_wa(int *IC_h, int *CP_h, int *S_h, float *sigma_h, int r,
+                                 int nz, int n, int repetition) {
+  return td_csc(IC_h, CP_h, S_h, sigma_h, r, nz, n, repetition);
+}
+
+extern "C" int bfs_gpu_bu_csc_sc(int *I_h, int *CP_h, int *S_h, int r, int nz, int n,
+                                 int repetition, int bbreak) {
+  (void)bbreak;
+  return bu_csc(I_h, CP_h, S_h, r, nz, n, repetition);
+}
+
+extern "C" int bfs_gpu_bu_csc_wa(int *I_h, int *CP_h, int *S_h, int r, int nz, int n,
+                                 int repetition, int bbreak) {
+  (void)bbreak;
+  return bu_csc(I_h, CP_h, S_h, r, nz, n, repetition);
+}
+
+extern "C" int bfs_gpu_tdbu_csc_sc(int *I_h, int *CP_h, int *S_h, int *sigma_h, int r,
+                                   int nz, int n, int repetition, int bbreak) {
+  (void)bbreak;
+  return tdbu_csc(I_h, CP_h, S_h, sigma_h, r, nz, n, repetition);
+}
+
+extern "C" int bfs_gpu_tdbu_csc_wa(int *IC_h, int *CP_h, int *S_h, int *sigma_h, int r,
+                                   int nz, int n, int repetition, int bbreak) {
+  (void)bbreak;
+  return tdbu_csc(IC_h, CP_h, S_h, sigma_h, r, nz, n, repetition);
+}
+
+extern "C" int bfs_gpu_td_cooc_sc(int *I_h, int *J_h, float *sigma_h, int r, int nz, int n,
+                                  int repetition) {
+  if (!sigma_h) return TBFS_ERR_INVALID_ARG;
+  CompatRun run;
+  int st = compat_run(I_h, J_h, true, r, nz, n, repetition, true, run);
+  if (st == TBFS_OK)
+    for (int v = 0; v < n; ++v) sigma_h[v] = (float)run.sigma[v];
+  return st;
+}
