@@ -115,6 +115,29 @@ tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_t k,
                           const tbfs_options *opt, int32_t *S, int64_t *sigma,
                           tbfs_stats *stats);
 
+/* One BFS that allocates nothing.  No counterpart in the reference: it is
+ * for callers that must not have a library call cudaMalloc or cudaFree --
+ * code running under a host framework that owns all device memory through
+ * its own pool, or a latency-critical loop that cannot take the device-wide
+ * synchronisation those calls may cause.  Every pointer is a device pointer
+ * the caller owns: the CSC in-lists, optionally separate out-lists
+ * (d_out_ptr/d_out_idx; NULL for a symmetric graph), S[n] and sigma[n]
+ * (sigma may be NULL for depths only).  Scratch (frontier queues, control
+ * block) is a static device array inside the library sized for at most
+ * TBFS_NOALLOC_MAX_VERTICES vertices (about 16 MB held on every GPU that
+ * loads the library, until exit); larger n is rejected with
+ * TBFS_ERR_UNSUPPORTED.  The first call on a device looks up that array's
+ * device address, so make it before any stream capture.  All calls share the
+ * array: calls whose GPU work overlaps race.  The input is validated on the
+ * device each call; the call returns after the traversal finished on
+ * `stream` (NULL = legacy default stream); stats->device_ms is left 0. */
+#define TBFS_NOALLOC_MAX_VERTICES (1 << 20)
+tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t *d_row_idx,
+                             const int32_t *d_out_ptr, const int32_t *d_out_idx,
+                             int32_t n, int64_t nnz, int32_t root, int32_t mode,
+                             int32_t *d_S, int64_t *d_sigma, void *stream,
+                             tbfs_stats *stats);
+
 /* Page-locked host buffers for fast host<->device copies. */
 tbfs_status tbfs_host_alloc_pinned(size_t bytes, void **ptr);
 void tbfs_host_free_pinned(void *ptr);

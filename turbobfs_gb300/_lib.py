@@ -82,6 +82,9 @@ _SIGNATURES = {
     "tbfs_graph_last_stats": (c_int, [c_void_p, POINTER(Stats)]),
     "tbfs_bfs_many": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), _P_I32, _P_I64,
                               POINTER(Stats)]),
+    "tbfs_bfs_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64,
+                                 c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                 POINTER(Stats)]),
     "tbfs_host_alloc_pinned": (c_int, [c_size_t, POINTER(c_void_p)]),
     "tbfs_host_free_pinned": (None, [c_void_p]),
     "tbfs_status_string": (c_char_p, [c_int]),
