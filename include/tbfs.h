@@ -50,6 +50,10 @@ typedef enum tbfs_mode {
 /* tbfs_graph_create_* flags */
 #define TBFS_GRAPH_SYMMETRIC 0x1u   /* caller guarantees in-lists == out-lists */
 #define TBFS_GRAPH_DEVICE_PTRS 0x2u /* input arrays are device pointers       */
+#define TBFS_GRAPH_KEEP_ORDER 0x4u  /* do not regroup vertices by degree; by
+                                       default hub vertices are renumbered to
+                                       the front inside the library (results
+                                       are always in the caller's numbering) */
 
 typedef struct tbfs_graph tbfs_graph;
 
@@ -65,6 +69,17 @@ typedef struct tbfs_options {
   float beta;                /* BU->TD when frontier size < n/beta           */
   void *stream;              /* cudaStream_t; NULL = legacy default stream   */
   int64_t timeout_ns;        /* grid-barrier wait budget; <=0 = 2 s          */
+  /* Per-level trace (host memory, may be NULL): record d holds
+   * {start ns (device globaltimer), frontier vertices, frontier out-edges,
+   *  direction 0 = top-down / 1 = bottom-up}; one extra record {end ns, 0,
+   *  0, -1} closes the run.  Capacity counts records (4 int64 each). */
+  int64_t *level_trace;
+  int32_t level_trace_cap;
+  /* Path counts of a level found bottom-up are finished one level later,
+   * either by pulling over that level's lists or by pushing from the
+   * previous level's lists; pull is used unless it reads more than
+   * pull_ratio times as many list entries as push.  <= 0: default 4. */
+  float pull_ratio;
 } tbfs_options;
 
 typedef struct tbfs_stats {
@@ -124,7 +139,7 @@ tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_t k,
  * (d_out_ptr/d_out_idx; NULL for a symmetric graph), S[n] and sigma[n]
  * (sigma may be NULL for depths only).  Scratch (frontier queues, control
  * block) is a static device array inside the library sized for at most
- * TBFS_NOALLOC_MAX_VERTICES vertices (about 16 MB held on every GPU that
+ * TBFS_NOALLOC_MAX_VERTICES vertices (about 36 MB held on every GPU that
  * loads the library, until exit); larger n is rejected with
  * TBFS_ERR_UNSUPPORTED.  The first call on a device looks up that array's
  * device address, so make it before any stream capture.  All calls share the

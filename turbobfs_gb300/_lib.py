@@ -26,6 +26,7 @@ STATUS_NAMES = {
 }
 GRAPH_SYMMETRIC = 0x1
 GRAPH_DEVICE_PTRS = 0x2
+GRAPH_KEEP_ORDER = 0x4
 BUILD_SYMMETRIZE, BUILD_DROP_LOOPS, BUILD_DEDUP, BUILD_SORT = 0x1, 0x2, 0x4, 0x8
 
 
@@ -39,6 +40,9 @@ class Options(ctypes.Structure):
         ("beta", c_float),
         ("stream", c_void_p),
         ("timeout_ns", c_int64),
+        ("level_trace", POINTER(c_int64)),
+        ("level_trace_cap", c_int32),
+        ("pull_ratio", c_float),
     ]
 
 

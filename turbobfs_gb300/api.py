@@ -18,7 +18,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import GRAPH_SYMMETRIC, Options, Stats, check, lib
+from ._lib import GRAPH_KEEP_ORDER, GRAPH_SYMMETRIC, Options, Stats, check, lib
 
 MODES = {"auto": 0, "do": 0, "td": 1, "top_down": 1, "bu": 2, "bottom_up": 2}
 _P_I32 = ctypes.POINTER(ctypes.c_int32)
@@ -37,8 +37,13 @@ def _ptr(a: np.ndarray, typ):
     return a.ctypes.data_as(typ)
 
 
+def _flags(symmetric: bool, keep_order: bool) -> int:
+    return (GRAPH_SYMMETRIC if symmetric else 0) | (GRAPH_KEEP_ORDER if keep_order else 0)
+
+
 def make_options(mode="auto", sigma=True, alpha=None, beta=None, timeout_ns=0,
-                 outputs_on_device=False, stream=None, inject_barrier_skip=0) -> Options:
+                 outputs_on_device=False, stream=None, inject_barrier_skip=0,
+                 pull_ratio=None) -> Options:
     o = Options()
     lib().tbfs_options_init(ctypes.byref(o))
     o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
@@ -51,6 +56,8 @@ def make_options(mode="auto", sigma=True, alpha=None, beta=None, timeout_ns=0,
     o.timeout_ns = int(timeout_ns)
     o.stream = stream
     o.inject_barrier_skip = int(inject_barrier_skip)
+    if pull_ratio is not None:
+        o.pull_ratio = float(pull_ratio)
     return o
 
 
@@ -64,29 +71,30 @@ class BfsResult:
 class Graph:
     """A graph resident in GPU memory until ``close()``."""
 
-    def __init__(self, col_ptr, row_idx, n: int | None = None, symmetric: bool = False):
+    def __init__(self, col_ptr, row_idx, n: int | None = None, symmetric: bool = False,
+                 keep_order: bool = False):
         cp, ic = _i32(col_ptr), _i32(row_idx)
         self.n = int(n if n is not None else cp.shape[0] - 1)
         self.nnz = int(ic.shape[0])
         self.symmetric = bool(symmetric)
         h = ctypes.c_void_p()
         check(lib().tbfs_graph_create_csc(_ptr(cp, _P_I32), _ptr(ic, _P_I32), self.n, self.nnz,
-                                          GRAPH_SYMMETRIC if symmetric else 0, ctypes.byref(h)),
+                                          _flags(symmetric, keep_order), ctypes.byref(h)),
               "tbfs_graph_create_csc")
         self._h = h
 
     @classmethod
-    def from_host_csc(cls, g) -> "Graph":
-        return cls(g.col_ptr, g.row_idx, g.n, symmetric=g.symmetric)
+    def from_host_csc(cls, g, keep_order: bool = False) -> "Graph":
+        return cls(g.col_ptr, g.row_idx, g.n, symmetric=g.symmetric, keep_order=keep_order)
 
     @classmethod
-    def from_cooc(cls, I, J, n: int, symmetric: bool = False) -> "Graph":
+    def from_cooc(cls, I, J, n: int, symmetric: bool = False, keep_order: bool = False) -> "Graph":
         I, J = _i32(I), _i32(J)
         self = cls.__new__(cls)
         self.n, self.nnz, self.symmetric = int(n), int(I.shape[0]), bool(symmetric)
         h = ctypes.c_void_p()
         check(lib().tbfs_graph_create_cooc(_ptr(I, _P_I32), _ptr(J, _P_I32), self.n, self.nnz,
-                                           GRAPH_SYMMETRIC if symmetric else 0, ctypes.byref(h)),
+                                           _flags(symmetric, keep_order), ctypes.byref(h)),
               "tbfs_graph_create_cooc")
         self._h = h
         return self
@@ -97,15 +105,37 @@ class Graph:
             raise RuntimeError("graph is closed")
         return self._h
 
-    def bfs(self, root: int, mode="auto", sigma: bool = True, **kw) -> BfsResult:
+    def bfs(self, root: int, mode="auto", sigma: bool = True, trace: int = 0,
+            **kw) -> BfsResult:
+        """One traversal.  trace=k records up to k-1 levels: stats["trace"]
+        lists {level, start_us, vertices, edges, direction ("td"/"bu")} with
+        start_us relative to the first level, and stats["trace_end_us"]."""
         o = make_options(mode, sigma, **kw)
         S = np.empty(self.n, dtype=np.int32)
         sg = np.empty(self.n, dtype=np.int64) if sigma else None
+        tr = None
+        if trace:
+            tr = np.zeros((max(int(trace), 2), 4), dtype=np.int64)
+            o.level_trace = tr.ctypes.data_as(_P_I64)
+            o.level_trace_cap = tr.shape[0]
         st = Stats()
         check(lib().tbfs_bfs(self.handle, int(root), ctypes.byref(o), _ptr(S, _P_I32),
                              _ptr(sg, _P_I64) if sg is not None else None, ctypes.byref(st)),
               "tbfs_bfs")
-        return BfsResult(S, sg, st.as_dict())
+        stats = st.as_dict()
+        if tr is not None:
+            t0 = tr[0, 0]
+            recs, end = [], None
+            for d, (t, qn, qe, dr) in enumerate(tr.tolist()):
+                if dr == -1:
+                    end = (t - t0) / 1e3
+                    break
+                if t == 0:
+                    break
+                recs.append({"level": d, "start_us": (t - t0) / 1e3, "vertices": qn,
+                             "edges": qe, "direction": "bu" if dr == 1 else "td"})
+            stats["trace"], stats["trace_end_us"] = recs, end
+        return BfsResult(S, sg, stats)
 
     def bfs_many(self, roots, mode="auto", sigma: bool = True, **kw):
         roots = _i32(roots)

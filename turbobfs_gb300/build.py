@@ -53,27 +53,36 @@ def _run(cmd: list[str], verbose: bool) -> str:
     return res.stdout + res.stderr
 
 
-def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = False) -> Path:
-    """Compile and link libtbfs.so if any source changed; return its path."""
+def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = False,
+          defines: dict | None = None, lib_path: Path | None = None,
+          build_dir: Path | None = None) -> Path:
+    """Compile and link libtbfs.so if any source changed; return its path.
+
+    `defines` sets the engine's compile-time tuning knobs (TBFS_EPT edges per
+    lane per round, TBFS_BLOCK threads per CTA, TBFS_MIN_BLOCKS); a tuned
+    variant is normally linked to its own `lib_path` / `build_dir`."""
     nvcc = nvcc_path()
-    BUILD.mkdir(exist_ok=True)
+    lib = Path(lib_path) if lib_path else LIB
+    bdir = Path(build_dir) if build_dir else BUILD
+    bdir.mkdir(parents=True, exist_ok=True)
     headers = _headers()
     jobs = []
     objs = []
     inc = [f"-I{INCLUDE}", f"-I{CSRC}"]
+    dflags = [f"-D{k}={v}" for k, v in sorted((defines or {}).items())]
     for src in CU_SOURCES:
         s = CSRC / src
-        o = BUILD / (src + ".o")
+        o = bdir / (src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                   "--expt-relaxed-constexpr", *inc, "-c", str(s), "-o", str(o)]
+                   "--expt-relaxed-constexpr", *dflags, *inc, "-c", str(s), "-o", str(o)]
             if ptxas_verbose:
                 cmd.insert(3, "-Xptxas=-v")
             jobs.append(cmd)
     for src in C_SOURCES:
         s = CSRC / src
-        o = BUILD / (src + ".o")
+        o = bdir / (src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(["gcc", "-O3", "-std=gnu11", "-fPIC", "-Wall", "-Wextra",
@@ -82,14 +91,14 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             outputs = list(ex.map(lambda c: _run(c, verbose), jobs))
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB.with_suffix(".so.tmp")
+    if force or jobs or _stale(lib, objs):
+        tmp = lib.with_suffix(".so.tmp")
         _run([nvcc, ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"], verbose)
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
     if ptxas_verbose:
         for out in outputs:
             sys.stdout.write(out)
-    return LIB
+    return lib
 
 
 def build_oracle(verbose: bool = False) -> Path:

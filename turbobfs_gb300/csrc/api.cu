@@ -79,6 +79,7 @@ extern "C" void tbfs_options_init(tbfs_options *opt) {
   opt->want_sigma = 1;
   opt->alpha = 15.0f;
   opt->beta = 18.0f;
+  opt->pull_ratio = 4.0f;
 }
 
 extern "C" tbfs_status tbfs_host_alloc_pinned(size_t bytes, void **ptr) {
@@ -105,13 +106,15 @@ static void graph_free(tbfs_graph *g) {
   }
   cudaFree(g->cp);
   cudaFree(g->ic);
-  cudaFree(g->q0);
-  cudaFree(g->q1);
-  cudaFree(g->e0);
-  cudaFree(g->e1);
+  cudaFree(g->queues);
+  cudaFree(g->bitmaps);
+  cudaFree(g->inv);
+  cudaFree(g->S_work);
+  cudaFree(g->sigma_work);
   cudaFree(g->ctl);
   cudaFree(g->S_dev);
   cudaFree(g->sigma_dev);
+  cudaFree(g->trace_dev);
   if (g->ctl_host) cudaFreeHost(g->ctl_host);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
@@ -135,10 +138,12 @@ static tbfs_status need_device() {
 /* allocations shared by both constructors, after cp/ic/rp/jr are set */
 static tbfs_status graph_finish(tbfs_graph *g) {
   const size_t n = (size_t)g->n;
-  CUDA_TRY(cudaMalloc(&g->q0, n * sizeof(int)));
-  CUDA_TRY(cudaMalloc(&g->q1, n * sizeof(int)));
-  CUDA_TRY(cudaMalloc(&g->e0, n * sizeof(int)));
-  CUDA_TRY(cudaMalloc(&g->e1, n * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->queues, 9 * n * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&g->bitmaps, 4 * ((n + 31) / 32) * sizeof(unsigned)));
+  if (g->inv) {
+    CUDA_TRY(cudaMalloc(&g->S_work, n * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&g->sigma_work, n * sizeof(unsigned long long)));
+  }
   CUDA_TRY(cudaMalloc(&g->ctl, sizeof(BfsCtl)));
   CUDA_TRY(cudaMallocHost(&g->ctl_host, sizeof(BfsCtl)));
   memset(g->ctl_host, 0, sizeof(BfsCtl));
@@ -171,6 +176,38 @@ static tbfs_status build_csc(tbfs_graph *g, const int32_t *col_ptr, const int32_
   if (st != TBFS_OK) return st;
   if (flag & 1) return invalid("col_ptr must start at 0, be nondecreasing and end at nnz");
   if (flag & 2) return invalid("row index outside [0, n)");
+  return TBFS_OK;
+}
+
+/* After the validated in-lists (cp, ic) are on the device: regroup the
+ * vertices by degree unless the caller asked to keep the order, then alias
+ * (symmetric) or build the out-lists as the transpose. */
+static tbfs_status finish_lists(tbfs_graph *g, int *d_flag) {
+  const size_t n = (size_t)g->n, nnz = (size_t)g->nnz;
+  if (!(g->flags & TBFS_GRAPH_KEEP_ORDER) && nnz > 0) {
+    int *perm = nullptr, *inv = nullptr, *cp2 = nullptr, *ic2 = nullptr;
+    bool identity = true;
+    cudaError_t e = cudaMalloc(&perm, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&inv, n * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&cp2, (n + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&ic2, nnz * sizeof(int));
+    if (e == cudaSuccess)
+      e = tbfs::degree_group_relabel(g->cp, g->ic, g->n, g->nnz, perm, inv, cp2, ic2, &identity,
+                                     0);
+    cudaFree(perm);
+    if (e != cudaSuccess || identity) {
+      cudaFree(inv);
+      cudaFree(cp2);
+      cudaFree(ic2);
+      if (e != cudaSuccess) return cuda_fail(e, "degree grouping", __LINE__);
+    } else {
+      cudaFree(g->cp);
+      cudaFree(g->ic);
+      g->cp = cp2;
+      g->ic = ic2;
+      g->inv = inv;
+    }
+  }
   if (g->flags & TBFS_GRAPH_SYMMETRIC) {
     g->rp = g->cp;
     g->jr = g->ic;
@@ -211,6 +248,7 @@ extern "C" tbfs_status tbfs_graph_create_csc(const int32_t *col_ptr, const int32
     return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
   }
   st = build_csc(g, col_ptr, row_idx, d_flag);
+  if (st == TBFS_OK) st = finish_lists(g, d_flag);
   cudaFree(d_flag);
   if (st == TBFS_OK) st = graph_finish(g);
   if (st != TBFS_OK) {
@@ -237,16 +275,6 @@ static tbfs_status build_cooc(tbfs_graph *g, const int32_t *row, const int32_t *
   /* in-lists: key = column (target), value = row (source) */
   if (e == cudaSuccess)
     e = tbfs::counting_sort_lists(dc, dr, g->nnz, g->n, g->cp, g->ic, d_flag, 0);
-  if (e == cudaSuccess && !(g->flags & TBFS_GRAPH_SYMMETRIC)) {
-    g->separate_out = true;
-    e = cudaMalloc(&g->rp, (n + 1) * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&g->jr, (nnz ? nnz : 1) * sizeof(int));
-    if (e == cudaSuccess)
-      e = tbfs::counting_sort_lists(dr, dc, g->nnz, g->n, g->rp, g->jr, d_flag, 0);
-  } else if (e == cudaSuccess) {
-    g->rp = g->cp;
-    g->jr = g->ic;
-  }
   cudaFree(dr);
   cudaFree(dc);
   if (e != cudaSuccess) return cuda_fail(e, "COOC ingest", __LINE__);
@@ -254,7 +282,7 @@ static tbfs_status build_cooc(tbfs_graph *g, const int32_t *row, const int32_t *
   tbfs_status st = read_flag(d_flag, 0, &flag);
   if (st != TBFS_OK) return st;
   if (flag) return invalid("COOC entry outside [0, n)");
-  return TBFS_OK;
+  return finish_lists(g, d_flag);
 }
 
 extern "C" tbfs_status tbfs_graph_create_cooc(const int32_t *row, const int32_t *col,
@@ -316,6 +344,7 @@ static tbfs_options resolve_opts(const tbfs_options *in) {
   if (in) o = *in;
   if (o.alpha <= 0.0f) o.alpha = 15.0f;
   if (o.beta <= 0.0f) o.beta = 18.0f;
+  if (!(o.pull_ratio > 0.0f)) o.pull_ratio = 4.0f;
   return o;
 }
 
@@ -326,12 +355,17 @@ static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o,
   p.ic = g->ic;
   p.rp = g->rp;
   p.jr = g->jr;
-  p.S = S;
-  p.sigma = o.want_sigma ? sigma : nullptr;
-  p.q0 = g->q0;
-  p.q1 = g->q1;
-  p.e0 = g->e0;
-  p.e1 = g->e1;
+  p.inv = g->inv;
+  p.S_out = S;
+  p.sigma_out = o.want_sigma ? sigma : nullptr;
+  p.S = g->inv ? g->S_work : S;
+  p.sigma = o.want_sigma ? (g->inv ? g->sigma_work : sigma) : nullptr;
+  for (int b = 0; b < 3; ++b) {
+    p.q[b] = g->queues + (size_t)(0 + b) * g->n;
+    p.e[b] = g->queues + (size_t)(3 + b) * g->n;
+    p.a[b] = g->queues + (size_t)(6 + b) * g->n;
+  }
+  for (int b = 0; b < 4; ++b) p.fb[b] = g->bitmaps + (size_t)b * ((g->n + 31) / 32);
   p.ctl = g->ctl;
   p.out_edges_total = g->out_edges_total;
   p.timeout_ns = o.timeout_ns > 0 ? o.timeout_ns : 2000000000LL;
@@ -341,7 +375,10 @@ static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o,
   p.symmetric = g->separate_out ? 0 : 1;
   p.alpha = o.alpha;
   p.beta = o.beta;
+  p.pull_ratio = o.pull_ratio;
   p.inject_barrier_skip = o.inject_barrier_skip > 0 ? o.inject_barrier_skip : 0;
+  p.trace = nullptr;
+  p.trace_cap = 0;
   return p;
 }
 
@@ -415,10 +452,27 @@ extern "C" tbfs_status tbfs_bfs(tbfs_graph *g, int32_t root, const tbfs_options 
     S_dst = g->S_dev;
     sig_dst = g->sigma_dev;
   }
-  const BfsParams p = make_params(g, root, o, S_dst, sig_dst);
+  BfsParams p = make_params(g, root, o, S_dst, sig_dst);
+  const bool tracing = o.level_trace != nullptr && o.level_trace_cap >= 2;
+  if (tracing) {
+    if (g->trace_cap < o.level_trace_cap) {
+      cudaFree(g->trace_dev);
+      g->trace_dev = nullptr;
+      g->trace_cap = 0;
+      CUDA_TRY(cudaMalloc(&g->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long)));
+      g->trace_cap = o.level_trace_cap;
+    }
+    CUDA_TRY(cudaMemsetAsync(g->trace_dev, 0, (size_t)o.level_trace_cap * 4 * sizeof(long long), s));
+    p.trace = g->trace_dev;
+    p.trace_cap = o.level_trace_cap;
+  }
   if ((st = enqueue_bfs(g, p, s, g->ev0, g->ev1, g->ctl_host)) != TBFS_OK) return st;
   g->pending = true;
   g->last_stream = s;
+  if (tracing)
+    CUDA_TRY(cudaMemcpyAsync(o.level_trace, g->trace_dev,
+                             (size_t)o.level_trace_cap * 4 * sizeof(long long),
+                             cudaMemcpyDeviceToHost, s));
   if (!o.outputs_on_device) {
     CUDA_TRY(cudaMemcpyAsync(S, S_dst, (size_t)g->n * sizeof(int), cudaMemcpyDeviceToHost, s));
     if (o.want_sigma)

@@ -11,47 +11,88 @@
  * TurboBFS_CSC_BU/bfsgpubucsc_sc.cu:81-95, and the host-side switch of
  * TurboBFS_CSC_TDBU/bfsgputdbucsc_sc.cu:119-153 (managed float sizef).
  *
- * Level d (frontier F_d = vertices at depth d, held as a queue) does:
- *   top-down : edge-balanced push over the out-edges of F_d: an unvisited
+ * Level d (frontier F_d = vertices at depth d, held as a queue) discovers
+ * F_{d+1} either
+ *   top-down : edge-balanced push over the out-edges of F_d; an unvisited
  *              target is claimed with atomicCAS(S, -1, d+1) and appended to
- *              the next queue.
+ *              the next queue, or
  *   bottom-up: every unvisited vertex scans its in-list and stops at the
  *              first in-neighbour with S == d (early exit).
- *   sigma    : sigma[v] for v in F_d is pulled once, in this same phase, as
- *              the sum of sigma[u] over in-list entries u with S[u] == d-1.
- *              These parents were finished one barrier earlier, so the pull
- *              never races with discovery, and bottom-up may stop early even
- *              when path counts are wanted.  For symmetric graphs the pull
- *              is fused into the top-down push (one read of each list).
- * sigma is exact in uint64 arithmetic; any sum that reaches 2^63 sets
+ *
+ * Path counts.  sigma[v] = sum of sigma[u] over the entries u->v with
+ * S[u] = S[v]-1 (each such entry is a "parent edge").  The engine computes
+ * sigma(F_{d+1}) wherever it is cheapest:
+ *   - during a top-down discovery from F_d whose counts are final: every
+ *     parent edge of F_{d+1} is examined by the push anyway, so each edge
+ *     that lands on a vertex claimed at depth d+1 adds sigma[u] to it
+ *     (no extra list reads);
+ *   - otherwise (F_{d+1} was found bottom-up, which stops early) in the next
+ *     phase, by either pulling over the lists of F_{d+1} or pushing from the
+ *     lists of F_d -- whichever frontier has fewer edges.  The three most
+ *     recent queues are kept, so F_d is still available then.
+ * Counts are exact in uint64 arithmetic; any sum that reaches 2^63 sets
  * ctl->sigma_overflow (overflow is reported, never rounded).
+ *
+ * Edge-balanced expansion: each queue entry carries the vertex, the
+ * exclusive prefix of out-degrees (its offset in the level's flattened edge
+ * space) and the start of its list.  A warp takes a contiguous range of
+ * flattened edges, stages 128 queue entries at a time in shared memory, and
+ * every lane handles kEPT consecutive edges per round, so that many list
+ * reads, then that many depth gathers, are in flight per lane.
  *
  * Direction rule (device side; Beamer, Asanovic, Patterson, "Direction-
  * optimizing breadth-first search", SC 2012): leave top-down when the
  * frontier's out-edges exceed (unexplored edges)/alpha; return to top-down
  * when the frontier shrinks below n/beta.
  *
- * Memory model: S, sigma, the queues and the counters are written during
- * the kernel by other SMs, so they are read with ld.global.cg (L2) and never
- * through the non-coherent L1; read-only graph arrays use the L1 path.
+ * Memory model.  Queues and counters are read with ld.global.cg (L2).
+ * Depth and path-count gathers use ordinary (L1-cacheable) loads: every
+ * value a test acts on -- S == d-1, S == d, S == d+1 claimed earlier in this
+ * phase only through an atomic's return value, sigma of a finished level --
+ * was written before the last grid barrier, whose gpu-scope acquire makes it
+ * visible to every later load of the CTA.  A plain load can return a stale
+ * -1 for a vertex claimed during this phase; the engine then only attempts
+ * an atomicCAS, whose return value is authoritative.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "tbfs_internal.h"
 
+#ifndef TBFS_EPT
+#define TBFS_EPT 6
+#endif
+#ifndef TBFS_BLOCK
+#define TBFS_BLOCK 256
+#endif
+#ifndef TBFS_MIN_BLOCKS
+#define TBFS_MIN_BLOCKS 3 /* 3 CTAs of 256 per SM: 80 registers, no spills */
+#endif
+
 namespace tbfs {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int kBlock = 512;
+constexpr int kBlock = TBFS_BLOCK;
+constexpr int kWarps = kBlock / 32;
+constexpr int kWin = 128;          /* queue entries staged per warp window */
+constexpr int kEPT = TBFS_EPT;     /* most consecutive edges per lane/round */
 enum { DIR_TD = 0, DIR_BU = 1 };
 
-__device__ __forceinline__ unsigned lanemask_lt() {
-  unsigned m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
+/* what an expansion does with path counts */
+enum SigMode {
+  SIG_NONE = 0,     /* depths only                                          */
+  SIG_PULL = 1,     /* entries gather sigma from neighbours at depth d-1    */
+  SIG_PUSH_NEW = 2, /* entries add their sigma to targets claimed at d+1    */
+  SIG_PUSH_AT = 3   /* entries add their sigma to targets at depth `tgt`    */
+};
+
+struct WarpWin {
+  unsigned long long val[kWin]; /* PULL: accumulator; PUSH: entry's sigma   */
+  int v[kWin];                  /* vertex of the entry                      */
+  int a[kWin];                  /* list index of its first window edge      */
+  unsigned s[kWin + 1];         /* window-relative start of its edges       */
+};
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -79,6 +120,22 @@ __device__ __forceinline__ unsigned long long add_chk(unsigned long long a,
   const unsigned long long s = a + b;
   if (s < a || (s >> 63)) ovf = true;
   return s;
+}
+
+/* *acc += x for a 64-bit accumulator in shared memory, with two native
+ * 32-bit atomics: the low word's returned old value yields the carry, which
+ * is folded into the high word's add; the high word's returned old value
+ * detects sums reaching 2^63.  Exact modulo 2^64 under any interleaving. */
+__device__ __forceinline__ void smem_add64(unsigned long long *acc, unsigned long long x,
+                                           bool &ovf) {
+  unsigned *w = reinterpret_cast<unsigned *>(acc);
+  const unsigned xl = (unsigned)x, xh = (unsigned)(x >> 32);
+  const unsigned old_l = atomicAdd(w, xl);
+  const unsigned carry = (old_l + xl) < old_l ? 1u : 0u;
+  const unsigned add_h = xh + carry;
+  const unsigned old_h = atomicAdd(w + 1, add_h);
+  const unsigned new_h = old_h + add_h;
+  if (new_h < old_h || (new_h >> 31) || add_h < xh) ovf = true;
 }
 
 /* Grid-wide barrier.  Thread 0 of every CTA arrives on a counter; the last
@@ -124,39 +181,55 @@ __device__ bool grid_barrier(BfsCtl *ctl, long long timeout_ns, int level) {
   return s_ok != 0;
 }
 
-/* Append the lanes with take=true to queue (q, e) of the next level:
- * one 64-bit atomic per warp reserves (count << 32 | out-edge sum), so the
- * queue position and the edge offset come from the same reservation and
- * e[] stays the exclusive prefix of out-degrees in queue order.  Must be
- * called by all 32 lanes. */
-__device__ __forceinline__ void warp_append(bool take, int v, int deg, int *q, int *e,
-                                            unsigned long long *ctr) {
-  const unsigned m = __ballot_sync(FULL, take);
-  if (m == 0) return;
+/* Append, for every lane, the entries j < N with bit j of `take` set to the
+ * next level's queue (q, e, a): one 64-bit atomic per warp reserves
+ * (count << 32 | out-edge sum), so queue positions and edge offsets come from
+ * the same reservation and e[] stays the exclusive prefix of out-degrees in
+ * queue order.  Must be called by all 32 lanes. */
+template <int N>
+__device__ __forceinline__ void warp_append(unsigned take, const int (&vv)[N],
+                                            const int (&dg)[N], const int (&ad)[N], int *q,
+                                            int *e, int *a, unsigned long long *ctr) {
   const int lane = threadIdx.x & 31;
-  const int dv = take ? deg : 0;
-  int incl = dv;
+  const int cnt = __popc(take);
+  int dsum = 0;
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+    if ((take >> j) & 1u) dsum += dg[j];
+  int ic = cnt, id = dsum;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(FULL, incl, o);
-    if (lane >= o) incl += t;
+    const int tc = __shfl_up_sync(FULL, ic, o);
+    const int td = __shfl_up_sync(FULL, id, o);
+    if (lane >= o) {
+      ic += tc;
+      id += td;
+    }
   }
-  const int total = __shfl_sync(FULL, incl, 31);
-  const int leader = __ffs(m) - 1;
+  const int tot_c = __shfl_sync(FULL, ic, 31);
+  if (tot_c == 0) return;
+  const int tot_d = __shfl_sync(FULL, id, 31);
   unsigned long long base = 0;
-  if (lane == leader)
-    base = atomicAdd(ctr, ((unsigned long long)__popc(m) << 32) | (unsigned)total);
-  base = __shfl_sync(FULL, base, leader);
-  if (take) {
-    const unsigned pos = (unsigned)(base >> 32) + __popc(m & lanemask_lt());
-    q[pos] = v;
-    e[pos] = (int)((unsigned)base + (unsigned)(incl - dv));
+  if (lane == 31)
+    base = atomicAdd(ctr, ((unsigned long long)tot_c << 32) | (unsigned)tot_d);
+  base = __shfl_sync(FULL, base, 31);
+  unsigned pos = (unsigned)(base >> 32) + (unsigned)(ic - cnt);
+  unsigned eo = (unsigned)base + (unsigned)(id - dsum);
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    if ((take >> j) & 1u) {
+      q[pos] = vv[j];
+      e[pos] = (int)eo;
+      a[pos] = ad[j];
+      ++pos;
+      eo += (unsigned)dg[j];
+    }
   }
 }
 
 /* Largest i in [0, qn) with e[i] <= target (e nondecreasing, e[0] = 0).
  * 32-ary search: each step narrows the range 32x with one load per lane. */
-__device__ __forceinline__ int warp_find_owner(const int *e, unsigned qn, unsigned target) {
+__device__ __forceinline__ unsigned warp_find_owner(const int *e, unsigned qn, unsigned target) {
   const int lane = threadIdx.x & 31;
   unsigned lo = 0, hi = qn;
   while (hi - lo > 32) {
@@ -172,184 +245,324 @@ __device__ __forceinline__ int warp_find_owner(const int *e, unsigned qn, unsign
   const unsigned pidx = lo + lane;
   const bool pred = pidx < hi && (unsigned)__ldcg(e + pidx) <= target;
   const unsigned m = __ballot_sync(FULL, pred);
-  return (int)(lo + (31 - __clz(m)));
+  return lo + (31 - __clz(m));
 }
 
-/* One warp processes the flattened out-edge range [E0, E1) of the queue
- * (qc, ec): warp-level load-balanced search over windows of 32 queue
- * entries, one edge per lane per round, coalesced reads of the lists.
- * PUSH: claim unvisited targets.  SIGMA: pull sigma from depth-(d-1)
- * neighbours (valid only when in-lists == out-lists). */
-template <bool PUSH, bool SIGMA>
-__device__ __forceinline__ void lbs_chunk(const BfsParams &p, int d, const int *qc,
-                                          const int *ec, unsigned qn, unsigned qe,
-                                          unsigned E0, unsigned E1, int *qx, int *ex,
-                                          unsigned long long *ctr_next, bool &ovf) {
+/* A level's queue: entries i < qn with vertex q[i], edge offset e[i], list
+ * start a[i]; qe is the total of its out-degrees. */
+struct Queue {
+  const int *q, *e, *a;
+  unsigned qn, qe;
+};
+
+/* Output queue of the level being discovered. */
+struct NextQueue {
+  int *q, *e, *a;
+  unsigned long long *ctr;
+};
+
+__device__ __forceinline__ bool bit_of(const unsigned *bm, int v) {
+  return (bm[(unsigned)v >> 5] >> ((unsigned)v & 31u)) & 1u;
+}
+
+/* One warp expands the flattened out-edge range [E0, E1) of queue Q.
+ * DISC: claim unvisited targets at depth d+1 into `nx` (and bitmap nb).
+ * SIG: see SigMode (PULL is valid only when in-lists == out-lists; the push
+ * modes walk the out-lists, which hold exactly the parent edges of their
+ * targets).  Without DISC, membership of a neighbour in the level the mode
+ * needs (d-1 for PULL, tgt for PUSH_AT) is read from bitmap tb, one bit per
+ * vertex, instead of from S. */
+template <bool DISC, int SIG>
+__device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt, const Queue &Q,
+                                             unsigned E0, unsigned E1, unsigned ept,
+                                             const NextQueue &nx, const unsigned *tb,
+                                             unsigned *nb, WarpWin &w, bool &ovf) {
   const int lane = threadIdx.x & 31;
-  const int *__restrict__ adjp = p.rp;
-  const int *__restrict__ adji = p.jr;
-  unsigned i0 = (unsigned)warp_find_owner(ec, qn, E0);
+  unsigned i0 = warp_find_owner(Q.e, Q.qn, E0);
   unsigned pos = E0;
-  while (pos < E1 && i0 < qn) {
-    const unsigned idx = i0 + lane;
-    int v = 0, a = 0;
-    unsigned len = 0;
-    if (idx < qn) {
-      v = __ldcg(qc + idx);
-      const unsigned eb = (unsigned)__ldcg(ec + idx);
-      const unsigned ee = (idx + 1 < qn) ? (unsigned)__ldcg(ec + idx + 1) : qe;
+  while (pos < E1 && i0 < Q.qn) {
+    const unsigned nw = (Q.qn - i0) < (unsigned)kWin ? (Q.qn - i0) : (unsigned)kWin;
+    for (unsigned k = lane; k < nw; k += 32) {
+      const unsigned i = i0 + k;
+      const unsigned eb = (unsigned)__ldcg(Q.e + i);
       const unsigned b = eb > pos ? eb : pos;
-      const unsigned en = ee < E1 ? ee : E1;
-      if (en > b) {
-        len = en - b;
-        a = __ldg(adjp + v) + (int)(b - eb);
-      }
+      const unsigned bc = b < E1 ? b : E1;
+      const int v = __ldcg(Q.q + i);
+      w.v[k] = v;
+      w.a[k] = __ldcg(Q.a + i) + (int)(b - eb);
+      w.s[k] = bc - pos;
+      if (SIG == SIG_PULL) w.val[k] = 0ull;
+      if (SIG == SIG_PUSH_NEW || SIG == SIG_PUSH_AT) w.val[k] = p.sigma[v];
     }
-    unsigned incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned t = __shfl_up_sync(FULL, incl, o);
-      if (lane >= o) incl += t;
+    if (lane == 0) {
+      const unsigned ee = (i0 + nw < Q.qn) ? (unsigned)__ldcg(Q.e + i0 + nw) : Q.qe;
+      w.s[nw] = (ee < E1 ? ee : E1) - pos;
     }
-    const unsigned excl = incl - len;
-    const unsigned total = __shfl_sync(FULL, incl, 31);
-    unsigned long long acc = 0;
-    for (unsigned base = 0; base < total; base += 32) {
-      const unsigned t = base + lane;
-      int k = 0; /* window entry owning edge t: largest k with excl_k <= t */
+    __syncwarp();
+    const unsigned tot = w.s[nw];
+    const unsigned round = 32u * ept;
+    for (unsigned base = 0; base < tot; base += round) {
+      const unsigned t0 = base + (unsigned)lane * ept;
+      const unsigned tend = t0 + ept < tot ? t0 + ept : tot;
+      int u[kEPT], kk[kEPT];
+      unsigned valid = 0;
 #pragma unroll
-      for (int s = 16; s >= 1; s >>= 1) {
-        const unsigned xs = __shfl_sync(FULL, excl, k + s);
-        if (xs <= t) k += s;
+      for (int j = 0; j < kEPT; ++j) {
+        kk[j] = 0;
+        u[j] = 0;
       }
-      const int ak = __shfl_sync(FULL, a, k);
-      const unsigned xk = __shfl_sync(FULL, excl, k);
-      const bool active = t < total;
-      bool won = false;
-      int u = 0;
-      unsigned long long c = 0;
-      if (active) {
-        u = __ldg(adji + ak + (int)(t - xk));
-        const int su = __ldcg(p.S + u);
-        if (PUSH && su == -1) won = atomicCAS(p.S + u, -1, d + 1) == -1;
-        if (SIGMA && su == d - 1) c = __ldcg(p.sigma + u);
-      }
-      if (PUSH) {
-        int dg = 0;
-        if (won) dg = __ldg(p.rp + u + 1) - __ldg(p.rp + u);
-        warp_append(won, u, dg, qx, ex, ctr_next);
-      }
-      if (SIGMA) {
-        unsigned long long s = c; /* segmented inclusive scan keyed by k */
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned long long sv = __shfl_up_sync(FULL, s, o);
-          const int kv = __shfl_up_sync(FULL, k, o);
-          if (lane >= o && kv == k) s = add_chk(s, sv, ovf);
+      if (t0 < tot) {
+        unsigned lo = 0, hi = nw - 1; /* largest k with s[k] <= t0 */
+        while (lo < hi) {
+          const unsigned mid = (lo + hi + 1) >> 1;
+          if (w.s[mid] <= t0) lo = mid;
+          else hi = mid - 1;
         }
-        /* window entry `lane` collects the segment sum at its last lane */
-        const unsigned lo = excl > base ? excl : base;
-        const unsigned hi0 = excl + len;
-        const unsigned hi = hi0 < base + 32u ? hi0 : base + 32u;
-        const int tail = hi > lo ? (int)(hi - 1u - base) : 0;
-        const unsigned long long got = __shfl_sync(FULL, s, tail);
-        if (hi > lo) acc = add_chk(acc, got, ovf);
+        unsigned k = lo;
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          const unsigned t = t0 + j;
+          if (t < tend) {
+            while (w.s[k + 1] <= t) ++k;
+            u[j] = w.a[k] + (int)(t - w.s[k]);
+            kk[j] = (int)k;
+            valid |= 1u << j;
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kEPT; ++j) /* list reads, all in flight */
+        if ((valid >> j) & 1u) u[j] = __ldg(p.jr + u[j]);
+      int su[kEPT];   /* DISC: depth of the neighbour                        */
+      unsigned in = 0; /* bit j: neighbour j is in the level the sigma mode needs */
+      if (DISC) {
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) su[j] = ((valid >> j) & 1u) ? p.S[u[j]] : -2;
+        if (SIG == SIG_PULL) {
+#pragma unroll
+          for (int j = 0; j < kEPT; ++j)
+            if (su[j] == d - 1) in |= 1u << j;
+        }
+      } else {
+        unsigned wd[kEPT];
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          su[j] = -2;
+          wd[j] = ((valid >> j) & 1u) ? tb[(unsigned)u[j] >> 5] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j)
+          if ((wd[j] >> ((unsigned)u[j] & 31u)) & 1u) in |= 1u << j;
+      }
+      unsigned hit = 0; /* PUSH_NEW: targets at depth d+1 after this edge */
+      if (DISC) {
+        unsigned take = 0;
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          if (su[j] == -1) {
+            const int old = atomicCAS(p.S + u[j], -1, d + 1);
+            if (old == -1) take |= 1u << j;
+            else if (old == d + 1) hit |= 1u << j;
+          } else if (su[j] == d + 1) {
+            hit |= 1u << j;
+          }
+        }
+        hit |= take;
+        int dg[kEPT], ad[kEPT];
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          ad[j] = 0;
+          dg[j] = 0;
+          if ((take >> j) & 1u) {
+            ad[j] = __ldg(p.rp + u[j]);
+            dg[j] = __ldg(p.rp + u[j] + 1) - ad[j];
+            atomicOr(nb + ((unsigned)u[j] >> 5), 1u << ((unsigned)u[j] & 31u));
+          }
+        }
+        warp_append<kEPT>(take, u, dg, ad, nx.q, nx.e, nx.a, nx.ctr);
+      }
+      if (SIG == SIG_PUSH_NEW || SIG == SIG_PUSH_AT) {
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          const bool add = SIG == SIG_PUSH_NEW ? ((hit >> j) & 1u) != 0 : ((in >> j) & 1u) != 0;
+          if (add) {
+            const unsigned long long x = w.val[kk[j]];
+            add_chk(atomicAdd(p.sigma + u[j], x), x, ovf);
+          }
+        }
+      }
+      if (SIG == SIG_PULL) {
+        unsigned long long c[kEPT]; /* path counts of the parents only */
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) c[j] = ((in >> j) & 1u) ? p.sigma[u[j]] : 0ull;
+        unsigned long long run = 0;
+        int rk = kk[0];
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          if (kk[j] != rk) {
+            if (run) smem_add64(&w.val[rk], run, ovf);
+            rk = kk[j];
+            run = 0;
+          }
+          run = add_chk(run, c[j], ovf);
+        }
+        if (run) smem_add64(&w.val[rk], run, ovf);
       }
     }
-    if (SIGMA && acc != 0) {
-      const unsigned long long old = atomicAdd(p.sigma + v, acc);
-      add_chk(old, acc, ovf);
+    __syncwarp();
+    if (SIG == SIG_PULL) {
+      for (unsigned k = lane; k < nw; k += 32) {
+        const unsigned long long x = w.val[k];
+        if (x) add_chk(atomicAdd(p.sigma + w.v[k], x), x, ovf);
+      }
     }
-    pos += total;
-    i0 += 32;
+    __syncwarp();
+    pos += tot;
+    i0 += nw;
   }
 }
 
-/* sigma for F_d over in-lists, one warp per frontier vertex (used when the
- * graph is not symmetric, so the push lists cannot serve the pull). */
-__device__ void sigma_pull_vertexwise(const BfsParams &p, int d, const int *qc,
-                                      unsigned qn, unsigned gwarp, unsigned nwarps,
-                                      bool &ovf) {
-  const int lane = threadIdx.x & 31;
-  for (unsigned i = gwarp; i < qn; i += nwarps) {
-    const int v = __ldcg(qc + i);
-    const int kb = __ldg(p.cp + v), ke = __ldg(p.cp + v + 1);
-    unsigned long long s = 0;
-    for (int k = kb + lane; k < ke; k += 32) {
-      const int u = __ldg(p.ic + k);
-      if (__ldcg(p.S + u) == d - 1) s = add_chk(s, __ldcg(p.sigma + u), ovf);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s = add_chk(s, __shfl_xor_sync(FULL, s, o), ovf);
-    if (lane == 0) p.sigma[v] = s;
+/* All warps of the grid expand queue Q, split into edge-balanced chunks.
+ * Small frontiers use fewer edges per lane (down to one), so their work is
+ * spread over more warps and each lane's chain of dependent loads is short;
+ * large frontiers use kEPT for memory-level parallelism. */
+template <bool DISC, int SIG>
+__device__ __forceinline__ void expand_level(const BfsParams &p, int d, int tgt, const Queue &Q,
+                                             const NextQueue &nx, const unsigned *tb,
+                                             unsigned *nb, unsigned gwarp, unsigned nwarps,
+                                             WarpWin &w, bool &ovf) {
+  const unsigned per_lane = (Q.qe + 32u * nwarps - 1) / (32u * nwarps);
+  const unsigned ept = per_lane < 1u ? 1u : (per_lane > (unsigned)kEPT ? (unsigned)kEPT : per_lane);
+  const unsigned round = 32u * ept;
+  unsigned ch = (Q.qe + nwarps - 1) / nwarps;
+  ch = (ch + round - 1) / round * round;
+  if (ch < round) ch = round;
+  if (ch > 16u * round) ch = 16u * round;
+  const unsigned nch = (Q.qe + ch - 1) / ch;
+  for (unsigned c = gwarp; c < nch; c += nwarps) {
+    const unsigned E0 = c * ch, E1 = E0 + ch < Q.qe ? E0 + ch : Q.qe;
+    expand_chunk<DISC, SIG>(p, d, tgt, Q, E0, E1, ept, nx, tb, nb, w, ovf);
   }
 }
 
-/* Bottom-up discovery: lane i of a warp owns vertex 32w+i; an unvisited
- * vertex scans its in-list until the first neighbour at depth d. */
-__device__ void bu_discover(const BfsParams &p, int d, int *qx, int *ex,
-                            unsigned long long *ctr, unsigned gwarp, unsigned nwarps) {
+/* Bottom-up discovery.  A warp takes kBuWords consecutive 32-vertex words
+ * per iteration; lane i owns vertex 32*word+i of each, so the depth checks,
+ * list bounds and the first gathers of all kBuWords vertices are in flight
+ * together.  An unvisited vertex scans its in-list until the first
+ * neighbour in F_d (bitmap cb); the scan advances every still-searching
+ * vertex of the lane by one entry per step.  The warp owns its words of the
+ * next level's bitmap nb and writes them whole. */
+constexpr int kBuWords = 8;
+
+__device__ void bu_discover(const BfsParams &p, int d, const NextQueue &nx, const unsigned *cb,
+                            unsigned *nb, unsigned gwarp, unsigned nwarps) {
   const int lane = threadIdx.x & 31;
   const unsigned nwords = ((unsigned)p.n + 31u) >> 5;
-  for (unsigned w = gwarp; w < nwords; w += nwarps) {
-    const int v = (int)(w * 32u + (unsigned)lane);
-    bool found = false;
-    if (v < p.n && __ldcg(p.S + v) == -1) {
-      int k = __ldg(p.cp + v);
-      const int ke = __ldg(p.cp + v + 1);
-      for (; k + 4 <= ke && !found; k += 4) { /* 4 independent gathers in flight */
-        const int u0 = __ldg(p.ic + k), u1 = __ldg(p.ic + k + 1);
-        const int u2 = __ldg(p.ic + k + 2), u3 = __ldg(p.ic + k + 3);
-        const int s0 = __ldcg(p.S + u0), s1 = __ldcg(p.S + u1);
-        const int s2 = __ldcg(p.S + u2), s3 = __ldcg(p.S + u3);
-        found = (s0 == d) | (s1 == d) | (s2 == d) | (s3 == d);
-      }
-      for (; k < ke && !found; ++k) found = __ldcg(p.S + __ldg(p.ic + k)) == d;
-      if (found) p.S[v] = d + 1;
+  const unsigned ntiles = (nwords + kBuWords - 1) / kBuWords;
+  for (unsigned tile = gwarp; tile < ntiles; tile += nwarps) {
+    int v[kBuWords], k[kBuWords], ke[kBuWords];
+    unsigned search = 0; /* bit j: vertex j unvisited and still searching */
+#pragma unroll
+    for (int j = 0; j < kBuWords; ++j) {
+      v[j] = (int)((tile * kBuWords + j) * 32u + (unsigned)lane);
+      k[j] = 0;
+      ke[j] = 0;
+      if (v[j] < p.n && p.S[v[j]] == -1) search |= 1u << j;
     }
-    const int dg = found ? (__ldg(p.rp + v + 1) - __ldg(p.rp + v)) : 0;
-    warp_append(found, v, dg, qx, ex, ctr);
+#pragma unroll
+    for (int j = 0; j < kBuWords; ++j)
+      if ((search >> j) & 1u) {
+        k[j] = __ldg(p.cp + v[j]);
+        ke[j] = __ldg(p.cp + v[j] + 1);
+      }
+    unsigned found = 0;
+    while (search) {
+      int u[kBuWords];
+#pragma unroll
+      for (int j = 0; j < kBuWords; ++j) {
+        if (((search >> j) & 1u) && k[j] >= ke[j]) search &= ~(1u << j); /* list exhausted */
+        u[j] = ((search >> j) & 1u) ? __ldg(p.ic + k[j]) : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < kBuWords; ++j) {
+        if ((search >> j) & 1u) {
+          if (bit_of(cb, u[j])) {
+            found |= 1u << j;
+            search &= ~(1u << j);
+          } else {
+            ++k[j];
+          }
+        }
+      }
+    }
+    int dg[kBuWords], ad[kBuWords];
+#pragma unroll
+    for (int j = 0; j < kBuWords; ++j) {
+      dg[j] = 0;
+      ad[j] = 0;
+      if ((found >> j) & 1u) {
+        p.S[v[j]] = d + 1;
+        ad[j] = __ldg(p.rp + v[j]);
+        dg[j] = __ldg(p.rp + v[j] + 1) - ad[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kBuWords; ++j) {
+      const unsigned word = __ballot_sync(FULL, (found >> j) & 1u);
+      const unsigned wi = tile * kBuWords + j;
+      if (lane == 0 && wi < nwords) nb[wi] = word;
+    }
+    warp_append<kBuWords>(found, v, dg, ad, nx.q, nx.e, nx.a, nx.ctr);
   }
 }
 
-__device__ __forceinline__ unsigned chunk_edges(unsigned qe, unsigned nwarps) {
-  unsigned ch = (qe + nwarps - 1) / nwarps;
-  ch = (ch + 31u) & ~31u;
-  if (ch < 64u) ch = 64u;
-  if (ch > 1024u) ch = 1024u;
-  return ch;
-}
-
-__global__ void __launch_bounds__(kBlock) bfs_persistent_kernel(const BfsParams p) {
+__global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel(const BfsParams p) {
+  __shared__ WarpWin s_win[kWarps];
+  WarpWin &win = s_win[threadIdx.x >> 5];
   const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned nthreads = gridDim.x * blockDim.x;
   const unsigned gwarp = gtid >> 5;
   const unsigned nwarps = nthreads >> 5;
   BfsCtl *ctl = p.ctl;
   const bool want_sigma = p.sigma != nullptr;
+  const int root = p.inv ? __ldg(p.inv + p.root) : p.root; /* internal numbering */
 
-  /* init: S = -1, sigma = 0, root at depth 0 with one path */
+  /* init: S = -1, sigma = 0, root at depth 0 with one path; F_0 = {root} in
+   * bitmap 0, the other bitmaps empty */
   for (unsigned i = gtid; i < (unsigned)p.n; i += nthreads) {
-    p.S[i] = (int)i == p.root ? 0 : -1;
-    if (want_sigma) p.sigma[i] = (int)i == p.root ? 1ull : 0ull;
+    p.S[i] = (int)i == root ? 0 : -1;
+    if (want_sigma) p.sigma[i] = (int)i == root ? 1ull : 0ull;
+  }
+  const unsigned nwords = ((unsigned)p.n + 31u) >> 5;
+  for (unsigned i = gtid; i < nwords; i += nthreads) {
+    p.fb[0][i] = i == ((unsigned)root >> 5) ? 1u << ((unsigned)root & 31u) : 0u;
+    p.fb[1][i] = 0u;
+    p.fb[2][i] = 0u;
+    p.fb[3][i] = 0u;
   }
   if (gtid == 0) {
-    p.q0[0] = p.root;
-    p.e0[0] = 0;
-    const unsigned deg = (unsigned)(__ldg(p.rp + p.root + 1) - __ldg(p.rp + p.root));
+    const int a = __ldg(p.rp + root);
+    p.q[0][0] = root;
+    p.e[0][0] = 0;
+    p.a[0][0] = a;
+    const unsigned deg = (unsigned)(__ldg(p.rp + root + 1) - a);
     ctl->qctr[0] = (1ull << 32) | deg;
   }
   if (!grid_barrier(ctl, p.timeout_ns, -1)) return;
 
   int d = 0, dir = DIR_TD, td = 0, bu = 0;
   long long m_u = p.out_edges_total, visited = 0, edges = 0;
-  unsigned prev_qn = 0;
-  bool ovf = false;
+  unsigned prev_qn = 0, prev_qe = 0;
+  bool ovf = false, sig_ready = true; /* sigma(F_d) final at the start of phase d */
+  bool done = false;
   for (;;) {
     const unsigned long long cur = __ldcg(&ctl->qctr[d % 3]);
     const unsigned qn = (unsigned)(cur >> 32);
     const unsigned qe = (unsigned)cur;
-    if (qn == 0) break;
+    if (qn == 0) {
+      done = true;
+      break;
+    }
     visited += qn;
     edges += qe;
     /* slot (d+2)%3 held F_{d-1}, read by every CTA before the last barrier;
@@ -366,59 +579,87 @@ __global__ void __launch_bounds__(kBlock) bfs_persistent_kernel(const BfsParams 
     } else if (qn < prev_qn && (double)qn <= (double)p.n / (double)p.beta) {
       dir = DIR_TD;
     }
-    prev_qn = qn;
+    if (gtid == 0 && p.trace && d < p.trace_cap - 1) {
+      long long *rec = p.trace + 4 * (long long)d;
+      rec[0] = (long long)global_ns();
+      rec[1] = qn;
+      rec[2] = qe;
+      rec[3] = dir;
+    }
 
-    const int *qc = (d & 1) ? p.q1 : p.q0;
-    const int *ec = (d & 1) ? p.e1 : p.e0;
-    int *qx = (d & 1) ? p.q0 : p.q1;
-    int *ex = (d & 1) ? p.e0 : p.e1;
-    unsigned long long *ctr_next = &ctl->qctr[(d + 1) % 3];
-    const bool sig = want_sigma && d > 0;
+    /* queues of levels d-1, d, d+1 rotate through three buffers */
+    const int bc = d % 3, bn = (d + 1) % 3, bp = (d + 2) % 3;
+    const Queue Qc = {p.q[bc], p.e[bc], p.a[bc], qn, qe};
+    const Queue Qp = {p.q[bp], p.e[bp], p.a[bp], prev_qn, prev_qe};
+    const NextQueue nx = {p.q[bn], p.e[bn], p.a[bn], &ctl->qctr[bn]};
+    /* bitmaps: F_{d-1}, F_d read; F_{d+1} written; F_{d+2}'s cleared (its
+     * previous contents, F_{d-2}, were last read in phase d-1) */
+    const unsigned *bm_prev = p.fb[(d + 3) % 4];
+    const unsigned *bm_cur = p.fb[d % 4];
+    unsigned *bm_next = p.fb[(d + 1) % 4];
+    unsigned *bm_clear = p.fb[(d + 2) % 4];
+    for (unsigned i = gtid; i < nwords; i += nthreads) bm_clear[i] = 0u;
+    bool next_ready = false;
 
     if (dir == DIR_TD) {
       ++td;
-      const unsigned ch = chunk_edges(qe, nwarps);
-      const unsigned nch = (qe + ch - 1) / ch;
-      if (sig && p.symmetric) {
-        for (unsigned c = gwarp; c < nch; c += nwarps) {
-          const unsigned E0 = c * ch, E1 = E0 + ch < qe ? E0 + ch : qe;
-          lbs_chunk<true, true>(p, d, qc, ec, qn, qe, E0, E1, qx, ex, ctr_next, ovf);
-        }
+      if (!want_sigma) {
+        expand_level<true, SIG_NONE>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win, ovf);
+      } else if (sig_ready) { /* parents final: counts ride on the push */
+        expand_level<true, SIG_PUSH_NEW>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win,
+                                         ovf);
+        next_ready = true;
+      } else if (p.symmetric) { /* finish sigma(F_d) on the same list reads */
+        expand_level<true, SIG_PULL>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win, ovf);
       } else {
-        for (unsigned c = gwarp; c < nch; c += nwarps) {
-          const unsigned E0 = c * ch, E1 = E0 + ch < qe ? E0 + ch : qe;
-          lbs_chunk<true, false>(p, d, qc, ec, qn, qe, E0, E1, qx, ex, ctr_next, ovf);
-        }
-        if (sig) sigma_pull_vertexwise(p, d, qc, qn, gwarp, nwarps, ovf);
+        expand_level<false, SIG_PUSH_AT>(p, d, d, Qp, nx, bm_cur, bm_next, gwarp, nwarps, win,
+                                         ovf);
+        expand_level<true, SIG_NONE>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win, ovf);
       }
     } else {
       ++bu;
-      if (sig) {
-        if (p.symmetric) {
-          const unsigned ch = chunk_edges(qe, nwarps);
-          const unsigned nch = (qe + ch - 1) / ch;
-          for (unsigned c = gwarp; c < nch; c += nwarps) {
-            const unsigned E0 = c * ch, E1 = E0 + ch < qe ? E0 + ch : qe;
-            lbs_chunk<false, true>(p, d, qc, ec, qn, qe, E0, E1, qx, ex, ctr_next, ovf);
-          }
-        } else {
-          sigma_pull_vertexwise(p, d, qc, qn, gwarp, nwarps, ovf);
-        }
+      if (want_sigma && !sig_ready) { /* sigma(F_d): pull unless push reads far less */
+        if (p.symmetric && (double)qe <= (double)p.pull_ratio * (double)prev_qe)
+          expand_level<false, SIG_PULL>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win,
+                                        ovf);
+        else
+          expand_level<false, SIG_PUSH_AT>(p, d, d, Qp, nx, bm_cur, bm_next, gwarp, nwarps, win,
+                                           ovf);
       }
-      bu_discover(p, d, qx, ex, ctr_next, gwarp, nwarps);
+      bu_discover(p, d, nx, bm_cur, bm_next, gwarp, nwarps);
     }
+    prev_qn = qn;
+    prev_qe = qe;
     /* test hook: CTA 0 leaves without arriving; the others' waits expire */
     if (p.inject_barrier_skip > 0 && blockIdx.x == 0 && d == p.inject_barrier_skip - 1) return;
     if (!grid_barrier(ctl, p.timeout_ns, d)) break;
+    sig_ready = next_ready;
     ++d;
   }
   if (__any_sync(FULL, ovf) && (threadIdx.x & 31) == 0) atomicOr(&ctl->sigma_overflow, 1);
+  /* results are final after the last barrier: gather them into the caller's
+   * numbering (coalesced writes, one gather per vertex) */
+  if (done && p.inv) {
+    for (unsigned i = gtid; i < (unsigned)p.n; i += nthreads) {
+      const int w = __ldg(p.inv + i);
+      p.S_out[i] = p.S[w];
+      if (want_sigma) p.sigma_out[i] = p.sigma[w];
+    }
+  }
   if (gtid == 0) {
     ctl->levels = d;
     ctl->td_levels = td;
     ctl->bu_levels = bu;
     ctl->visited = visited;
     ctl->edges = edges;
+    if (p.trace) {
+      const int slot = d < p.trace_cap - 1 ? d : p.trace_cap - 1;
+      long long *rec = p.trace + 4 * (long long)slot;
+      rec[0] = (long long)global_ns();
+      rec[1] = 0;
+      rec[2] = 0;
+      rec[3] = -1;
+    }
   }
 }
 
@@ -431,6 +672,11 @@ cudaError_t bfs_geometry(int device, LaunchGeom *out) {
   e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   if (e != cudaSuccess) return e;
   if (!coop) return cudaErrorNotSupported;
+  /* the kernel needs ~20 KB of shared memory per CTA; leave the rest of the
+   * unified L1/shared array to L1, which caches the depth/path-count gathers */
+  e = cudaFuncSetAttribute(bfs_persistent_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           25);
+  if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bfs_persistent_kernel, kBlock, 0);
   if (e != cudaSuccess) return e;
   if (per < 1) return cudaErrorInvalidConfiguration;

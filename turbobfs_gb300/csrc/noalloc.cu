@@ -11,7 +11,7 @@
  * control block the traversal needs live in one file-scope device array,
  * g_noalloc_scratch, sized for graphs of up to TBFS_NOALLOC_MAX_VERTICES
  * vertices.  That array is part of the library image: every GPU that loads
- * the library holds it (about 16 MB) until the process exits.
+ * the library holds it (about 36 MB) until the process exits.
  *
  * Host code cannot use the array's name as a device address; on the first
  * call on each device (with that device current) the address is looked up
@@ -33,7 +33,8 @@ namespace {
 
 constexpr size_t kCtlBytes = 1024; /* control block + validation flag */
 constexpr size_t kQueueBytes = (size_t)TBFS_NOALLOC_MAX_VERTICES * sizeof(int);
-constexpr size_t kScratchBytes = kCtlBytes + 4 * kQueueBytes;
+constexpr size_t kBitmapBytes = (size_t)TBFS_NOALLOC_MAX_VERTICES / 8;
+constexpr size_t kScratchBytes = kCtlBytes + 9 * kQueueBytes + 4 * kBitmapBytes;
 constexpr size_t kFlagOffset = 768;
 static_assert(sizeof(tbfs::BfsCtl) <= kFlagOffset, "control block must fit its slot");
 
@@ -131,10 +132,18 @@ extern "C" tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t 
   p.jr = jr;
   p.S = d_S;
   p.sigma = reinterpret_cast<unsigned long long *>(d_sigma);
-  p.q0 = q;
-  p.q1 = q + TBFS_NOALLOC_MAX_VERTICES;
-  p.e0 = q + 2 * (size_t)TBFS_NOALLOC_MAX_VERTICES;
-  p.e1 = q + 3 * (size_t)TBFS_NOALLOC_MAX_VERTICES;
+  p.inv = nullptr; /* the caller's numbering is used as is */
+  p.S_out = p.S;
+  p.sigma_out = p.sigma;
+  for (int b = 0; b < 3; ++b) {
+    p.q[b] = q + (size_t)(0 + b) * TBFS_NOALLOC_MAX_VERTICES;
+    p.e[b] = q + (size_t)(3 + b) * TBFS_NOALLOC_MAX_VERTICES;
+    p.a[b] = q + (size_t)(6 + b) * TBFS_NOALLOC_MAX_VERTICES;
+  }
+  for (int b = 0; b < 4; ++b)
+    p.fb[b] = reinterpret_cast<unsigned *>(base + kCtlBytes + 9 * kQueueBytes + b * kBitmapBytes);
+  p.trace = nullptr;
+  p.trace_cap = 0;
   p.ctl = ctl;
   p.out_edges_total = nnz;
   p.timeout_ns = 2000000000LL;
@@ -144,6 +153,7 @@ extern "C" tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t 
   p.symmetric = symmetric ? 1 : 0;
   p.alpha = 15.0f;
   p.beta = 18.0f;
+  p.pull_ratio = 4.0f;
   p.inject_barrier_skip = 0;
   if ((e = tbfs::bfs_launch(p, ds->geom, s)) != cudaSuccess) return cuda_fail(e, "launch");
   tbfs::BfsCtl c;

@@ -5,10 +5,15 @@
  *   cp[n+1], ic[nnz]   int32 CSC: in-lists (column v = sources of edges ->v)
  *   rp[n+1], jr[nnz]   int32 out-lists; aliases cp/ic when the graph is
  *                      symmetric, else the transpose built on the device
- * Per-traversal workspace (reused across calls on the same graph):
- *   q0[n], q1[n]       int32 frontier queues (ping-pong by level parity)
- *   e0[n], e1[n]       int32 out-edge offset of each queue entry (exclusive
+ * Per-traversal workspace (reused across calls on the same graph), three
+ * rotating buffers so that the queues of levels d-1, d and d+1 coexist:
+ *   q[3][n]            int32 frontier vertices
+ *   e[3][n]            int32 out-edge offset of each queue entry (exclusive
  *                      prefix of out-degrees, in queue order)
+ *   a[3][n]            int32 start of each queue entry's out-list (rp[v])
+ *   fb[4][n/32]        frontier bitmaps (bit v of fb[d % 4]: v in F_d); four so
+ *                      that F_{d-1} and F_d are read while F_{d+1} is written
+ *                      and F_{d+2}'s is cleared in the same phase
  *   ctl                control block: per-level counters, barrier words
  * Outputs: S[n] int32 (-1 unreached), sigma[n] uint64 bit patterns of the
  * int64 path counts.
@@ -45,13 +50,23 @@ struct BfsParams {
   const int *rp, *jr; /* out-lists */
   int *S;
   unsigned long long *sigma; /* null: S only */
-  int *q0, *q1, *e0, *e1;
+  int *q[3], *e[3], *a[3];   /* queue buffers; level d uses buffer d % 3 */
+  unsigned *fb[4];           /* frontier bitmaps; F_d in fb[d % 4]         */
   BfsCtl *ctl;
   long long out_edges_total;
   long long timeout_ns;
   int n, root, mode, symmetric;
   float alpha, beta;
+  float pull_ratio; /* see tbfs_options.pull_ratio */
   int inject_barrier_skip; /* test hook, 0 = off */
+  int trace_cap;           /* records in trace */
+  long long *trace;        /* device buffer of trace_cap x 4 int64, or null */
+  /* graph stored in its own numbering: inv[caller id] = internal id; S and
+   * sigma above are then internal work arrays and the results are gathered
+   * into S_out / sigma_out (caller order) at the end.  Null: identity. */
+  const int *inv;
+  int *S_out;
+  unsigned long long *sigma_out;
 };
 
 /* Launch geometry of the persistent kernel on the current device. */
@@ -70,6 +85,13 @@ cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
                                 int n, int *ptr_out, int *idx_out, int *d_flag,
                                 cudaStream_t s);
 cudaError_t expand_columns(const int *cp, int n, int *col_of_entry, cudaStream_t s);
+/* Degree-based grouping of the vertices (see graph_ingest.cu).  On return
+ * *identity tells whether the order is unchanged (then perm/inv/cp2/ic2 are
+ * untouched); otherwise perm[new] = old, inv[old] = new and (cp2, ic2) is the
+ * CSC with columns and row ids renamed. */
+cudaError_t degree_group_relabel(const int *cp, const int *ic, int n, long long nnz,
+                                 int *perm, int *inv, int *cp2, int *ic2, bool *identity,
+                                 cudaStream_t s);
 
 }  // namespace tbfs
 
@@ -83,11 +105,19 @@ struct tbfs_graph {
   bool separate_out = false;
   long long out_edges_total = 0;
   /* workspace */
-  int *q0 = nullptr, *q1 = nullptr, *e0 = nullptr, *e1 = nullptr;
+  int *queues = nullptr; /* one allocation: q[3], e[3], a[3], n ints each */
+  unsigned *bitmaps = nullptr; /* four frontier bitmaps, (n+31)/32 words each */
+  /* degree-grouped numbering: inv[caller id] = internal id (null: identity);
+   * the traversal works on internal S/sigma and un-permutes at the end */
+  int *inv = nullptr;
+  int *S_work = nullptr;
+  unsigned long long *sigma_work = nullptr;
   tbfs::BfsCtl *ctl = nullptr;
   tbfs::BfsCtl *ctl_host = nullptr; /* pinned mirror */
   int *S_dev = nullptr;
   unsigned long long *sigma_dev = nullptr;
+  long long *trace_dev = nullptr; /* per-level trace records */
+  int trace_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t last_stream = nullptr;
   tbfs::LaunchGeom geom;
