@@ -109,6 +109,7 @@ static void graph_free(tbfs_graph *g) {
   cudaFree(g->queues);
   cudaFree(g->bitmaps);
   cudaFree(g->inv);
+  cudaFree(g->perm);
   cudaFree(g->S_work);
   cudaFree(g->sigma_work);
   cudaFree(g->ctl);
@@ -194,8 +195,8 @@ static tbfs_status finish_lists(tbfs_graph *g, int *d_flag) {
     if (e == cudaSuccess)
       e = tbfs::degree_group_relabel(g->cp, g->ic, g->n, g->nnz, perm, inv, cp2, ic2, &identity,
                                      0);
-    cudaFree(perm);
     if (e != cudaSuccess || identity) {
+      cudaFree(perm);
       cudaFree(inv);
       cudaFree(cp2);
       cudaFree(ic2);
@@ -206,6 +207,7 @@ static tbfs_status finish_lists(tbfs_graph *g, int *d_flag) {
       g->cp = cp2;
       g->ic = ic2;
       g->inv = inv;
+      g->perm = perm;
     }
   }
   if (g->flags & TBFS_GRAPH_SYMMETRIC) {
@@ -356,6 +358,7 @@ static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o,
   p.rp = g->rp;
   p.jr = g->jr;
   p.inv = g->inv;
+  p.perm = g->perm;
   p.S_out = S;
   p.sigma_out = o.want_sigma ? sigma : nullptr;
   p.S = g->inv ? g->S_work : S;

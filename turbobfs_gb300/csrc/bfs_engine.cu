@@ -422,26 +422,69 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
   }
 }
 
-/* All warps of the grid expand queue Q, split into edge-balanced chunks.
+/* How one expansion of queue Q is cut into work items (edge chunks).
  * Small frontiers use fewer edges per lane (down to one), so their work is
  * spread over more warps and each lane's chain of dependent loads is short;
- * large frontiers use kEPT for memory-level parallelism. */
-template <bool DISC, int SIG>
-__device__ __forceinline__ void expand_level(const BfsParams &p, int d, int tgt, const Queue &Q,
-                                             const NextQueue &nx, const unsigned *tb,
-                                             unsigned *nb, unsigned gwarp, unsigned nwarps,
-                                             WarpWin &w, bool &ovf) {
-  const unsigned per_lane = (Q.qe + 32u * nwarps - 1) / (32u * nwarps);
-  const unsigned ept = per_lane < 1u ? 1u : (per_lane > (unsigned)kEPT ? (unsigned)kEPT : per_lane);
-  const unsigned round = 32u * ept;
-  unsigned ch = (Q.qe + nwarps - 1) / nwarps;
+ * large frontiers use kEPT for memory-level parallelism.  About four chunks
+ * per warp keep the dynamic scheduler balanced. */
+struct ExpandPlan {
+  unsigned ept, ch, nch;
+};
+
+__device__ __forceinline__ ExpandPlan plan_expand(unsigned qe, unsigned nwarps) {
+  ExpandPlan pl;
+  const unsigned per_lane = (qe + 32u * nwarps - 1) / (32u * nwarps);
+  pl.ept = per_lane < 1u ? 1u : (per_lane > (unsigned)kEPT ? (unsigned)kEPT : per_lane);
+  const unsigned round = 32u * pl.ept;
+  unsigned ch = (qe + 4u * nwarps - 1) / (4u * nwarps);
   ch = (ch + round - 1) / round * round;
   if (ch < round) ch = round;
   if (ch > 16u * round) ch = 16u * round;
-  const unsigned nch = (Q.qe + ch - 1) / ch;
-  for (unsigned c = gwarp; c < nch; c += nwarps) {
-    const unsigned E0 = c * ch, E1 = E0 + ch < Q.qe ? E0 + ch : Q.qe;
-    expand_chunk<DISC, SIG>(p, d, tgt, Q, E0, E1, ept, nx, tb, nb, w, ovf);
+  pl.ch = ch;
+  pl.nch = (qe + ch - 1) / ch;
+  return pl;
+}
+
+/* the expansions a phase can run (template instances of expand_chunk) */
+enum ExpandKind {
+  EX_NONE = 0,
+  EX_DISC = 1,          /* discovery, depths only                 */
+  EX_DISC_PUSH_NEW = 2, /* discovery + counts pushed to new targets */
+  EX_DISC_PULL = 3,     /* discovery + counts of the entries pulled */
+  EX_PUSH_AT = 4,       /* counts pushed to targets at depth tgt    */
+  EX_PULL = 5           /* counts of the entries pulled             */
+};
+
+struct ExpandTask {
+  int kind, tgt;
+  Queue Q;
+  const unsigned *tb;
+  ExpandPlan pl;
+};
+
+__device__ __forceinline__ void run_expand_item(const BfsParams &p, int d, const ExpandTask &t,
+                                                unsigned c, const NextQueue &nx, unsigned *nb,
+                                                WarpWin &w, bool &ovf) {
+  const unsigned E0 = c * t.pl.ch;
+  const unsigned E1 = E0 + t.pl.ch < t.Q.qe ? E0 + t.pl.ch : t.Q.qe;
+  switch (t.kind) {
+    case EX_DISC:
+      expand_chunk<true, SIG_NONE>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      break;
+    case EX_DISC_PUSH_NEW:
+      expand_chunk<true, SIG_PUSH_NEW>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      break;
+    case EX_DISC_PULL:
+      expand_chunk<true, SIG_PULL>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      break;
+    case EX_PUSH_AT:
+      expand_chunk<false, SIG_PUSH_AT>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      break;
+    case EX_PULL:
+      expand_chunk<false, SIG_PULL>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      break;
+    default:
+      break;
   }
 }
 
@@ -454,12 +497,11 @@ __device__ __forceinline__ void expand_level(const BfsParams &p, int d, int tgt,
  * next level's bitmap nb and writes them whole. */
 constexpr int kBuWords = 8;
 
-__device__ void bu_discover(const BfsParams &p, int d, const NextQueue &nx, const unsigned *cb,
-                            unsigned *nb, unsigned gwarp, unsigned nwarps) {
+__device__ void bu_tile(const BfsParams &p, int d, const NextQueue &nx, const unsigned *cb,
+                        unsigned *nb, unsigned tile) {
   const int lane = threadIdx.x & 31;
   const unsigned nwords = ((unsigned)p.n + 31u) >> 5;
-  const unsigned ntiles = (nwords + kBuWords - 1) / kBuWords;
-  for (unsigned tile = gwarp; tile < ntiles; tile += nwarps) {
+  {
     int v[kBuWords], k[kBuWords], ke[kBuWords];
     unsigned search = 0; /* bit j: vertex j unvisited and still searching */
 #pragma unroll
@@ -476,21 +518,23 @@ __device__ void bu_discover(const BfsParams &p, int d, const NextQueue &nx, cons
         ke[j] = __ldg(p.cp + v[j] + 1);
       }
     unsigned found = 0;
-    while (search) {
-      int u[kBuWords];
+    while (search) { /* two list entries per searching vertex per step */
+      int u0[kBuWords], u1[kBuWords];
 #pragma unroll
       for (int j = 0; j < kBuWords; ++j) {
         if (((search >> j) & 1u) && k[j] >= ke[j]) search &= ~(1u << j); /* list exhausted */
-        u[j] = ((search >> j) & 1u) ? __ldg(p.ic + k[j]) : 0;
+        const bool on = (search >> j) & 1u;
+        u0[j] = on ? __ldg(p.ic + k[j]) : 0;
+        u1[j] = (on && k[j] + 1 < ke[j]) ? __ldg(p.ic + k[j] + 1) : -1;
       }
 #pragma unroll
       for (int j = 0; j < kBuWords; ++j) {
         if ((search >> j) & 1u) {
-          if (bit_of(cb, u[j])) {
+          if (bit_of(cb, u0[j]) || (u1[j] >= 0 && bit_of(cb, u1[j]))) {
             found |= 1u << j;
             search &= ~(1u << j);
           } else {
-            ++k[j];
+            k[j] += 2;
           }
         }
       }
@@ -521,7 +565,6 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
   WarpWin &win = s_win[threadIdx.x >> 5];
   const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned nthreads = gridDim.x * blockDim.x;
-  const unsigned gwarp = gtid >> 5;
   const unsigned nwarps = nthreads >> 5;
   BfsCtl *ctl = p.ctl;
   const bool want_sigma = p.sigma != nullptr;
@@ -599,34 +642,49 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     unsigned *bm_next = p.fb[(d + 1) % 4];
     unsigned *bm_clear = p.fb[(d + 2) % 4];
     for (unsigned i = gtid; i < nwords; i += nthreads) bm_clear[i] = 0u;
+    /* work counter of phase d+2 (last used in phase d-2) */
+    if (gtid == 0) ctl->work[(d + 2) & 3] = 0u;
     bool next_ready = false;
 
+    /* this phase's work: up to two expansions, then bottom-up tiles */
+    ExpandTask A = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}};
+    ExpandTask B = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}};
     if (dir == DIR_TD) {
       ++td;
       if (!want_sigma) {
-        expand_level<true, SIG_NONE>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win, ovf);
+        A.kind = EX_DISC;
       } else if (sig_ready) { /* parents final: counts ride on the push */
-        expand_level<true, SIG_PUSH_NEW>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win,
-                                         ovf);
+        A.kind = EX_DISC_PUSH_NEW;
         next_ready = true;
       } else if (p.symmetric) { /* finish sigma(F_d) on the same list reads */
-        expand_level<true, SIG_PULL>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win, ovf);
-      } else {
-        expand_level<false, SIG_PUSH_AT>(p, d, d, Qp, nx, bm_cur, bm_next, gwarp, nwarps, win,
-                                         ovf);
-        expand_level<true, SIG_NONE>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win, ovf);
+        A.kind = EX_DISC_PULL;
+      } else { /* sigma(F_d) from F_{d-1}'s out-lists, discovery from F_d */
+        A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}};
+        B.kind = EX_DISC;
       }
     } else {
       ++bu;
       if (want_sigma && !sig_ready) { /* sigma(F_d): pull unless push reads far less */
         if (p.symmetric && (double)qe <= (double)p.pull_ratio * (double)prev_qe)
-          expand_level<false, SIG_PULL>(p, d, 0, Qc, nx, bm_prev, bm_next, gwarp, nwarps, win,
-                                        ovf);
+          A.kind = EX_PULL;
         else
-          expand_level<false, SIG_PUSH_AT>(p, d, d, Qp, nx, bm_cur, bm_next, gwarp, nwarps, win,
-                                           ovf);
+          A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}};
       }
-      bu_discover(p, d, nx, bm_cur, bm_next, gwarp, nwarps);
+    }
+    if (A.kind != EX_NONE) A.pl = plan_expand(A.Q.qe, nwarps);
+    if (B.kind != EX_NONE) B.pl = plan_expand(B.Q.qe, nwarps);
+    const unsigned n_tiles = dir == DIR_BU ? (nwords + kBuWords - 1) / kBuWords : 0u;
+    const unsigned n_a = A.pl.nch, n_ab = n_a + B.pl.nch, n_all = n_ab + n_tiles;
+    unsigned *wctr = &ctl->work[d & 3];
+    const int lane = threadIdx.x & 31;
+    for (;;) { /* dynamic scheduling: each warp claims the next work item */
+      unsigned item = 0;
+      if (lane == 0) item = atomicAdd(wctr, 1u);
+      item = __shfl_sync(FULL, item, 0);
+      if (item >= n_all) break;
+      if (item < n_a) run_expand_item(p, d, A, item, nx, bm_next, win, ovf);
+      else if (item < n_ab) run_expand_item(p, d, B, item - n_a, nx, bm_next, win, ovf);
+      else bu_tile(p, d, nx, bm_cur, bm_next, item - n_ab);
     }
     prev_qn = qn;
     prev_qe = qe;
@@ -637,13 +695,13 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     ++d;
   }
   if (__any_sync(FULL, ovf) && (threadIdx.x & 31) == 0) atomicOr(&ctl->sigma_overflow, 1);
-  /* results are final after the last barrier: gather them into the caller's
-   * numbering (coalesced writes, one gather per vertex) */
-  if (done && p.inv) {
+  /* results are final after the last barrier: scatter them into the
+   * caller's numbering (coalesced reads, stores need no round trip) */
+  if (done && p.perm) {
     for (unsigned i = gtid; i < (unsigned)p.n; i += nthreads) {
-      const int w = __ldg(p.inv + i);
-      p.S_out[i] = p.S[w];
-      if (want_sigma) p.sigma_out[i] = p.sigma[w];
+      const int o = __ldg(p.perm + i);
+      p.S_out[o] = p.S[i];
+      if (want_sigma) p.sigma_out[o] = p.sigma[i];
     }
   }
   if (gtid == 0) {

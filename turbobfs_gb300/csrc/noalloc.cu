@@ -133,6 +133,7 @@ extern "C" tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t 
   p.S = d_S;
   p.sigma = reinterpret_cast<unsigned long long *>(d_sigma);
   p.inv = nullptr; /* the caller's numbering is used as is */
+  p.perm = nullptr;
   p.S_out = p.S;
   p.sigma_out = p.sigma;
   for (int b = 0; b < 3; ++b) {

@@ -37,7 +37,8 @@ struct __align__(128) BfsCtl {
   int levels, td_levels, bu_levels;
   int timeout_level;   /* level + 2 of the barrier that gave up, else 0  */
   long long visited, edges;
-  unsigned int pad0[14];
+  unsigned int work[4]; /* dynamic work counter of phase d in work[d % 4] */
+  unsigned int pad0[10];
   /* barrier words on their own 128-byte lines */
   unsigned int bar_arrive;
   unsigned int pad1[31];
@@ -61,10 +62,12 @@ struct BfsParams {
   int inject_barrier_skip; /* test hook, 0 = off */
   int trace_cap;           /* records in trace */
   long long *trace;        /* device buffer of trace_cap x 4 int64, or null */
-  /* graph stored in its own numbering: inv[caller id] = internal id; S and
-   * sigma above are then internal work arrays and the results are gathered
-   * into S_out / sigma_out (caller order) at the end.  Null: identity. */
+  /* graph stored in its own numbering: inv[caller id] = internal id,
+   * perm[internal id] = caller id; S and sigma above are then internal work
+   * arrays, scattered into S_out / sigma_out (caller order) at the end.
+   * Null: identity. */
   const int *inv;
+  const int *perm;
   int *S_out;
   unsigned long long *sigma_out;
 };
@@ -110,6 +113,7 @@ struct tbfs_graph {
   /* degree-grouped numbering: inv[caller id] = internal id (null: identity);
    * the traversal works on internal S/sigma and un-permutes at the end */
   int *inv = nullptr;
+  int *perm = nullptr; /* perm[internal id] = caller id */
   int *S_work = nullptr;
   unsigned long long *sigma_work = nullptr;
   tbfs::BfsCtl *ctl = nullptr;
