@@ -130,6 +130,27 @@ tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_t k,
                           const tbfs_options *opt, int32_t *S, int64_t *sigma,
                           tbfs_stats *stats);
 
+/* Many roots on one graph in one frontier-matrix traversal: up to 256 roots
+ * advance together in one persistent launch (more are taken 256 at a time),
+ * every list read shared by all of them.  No counterpart in the reference,
+ * which runs one root per call; results are identical to k calls of
+ * tbfs_bfs (S: -1 unreached; sigma: exact int64 path counts, per-root
+ * overflow flag in stats[r].sigma_overflow).  Layout of S (k x n int32) and
+ * sigma (k x n int64, may be NULL for depths only):
+ *   TBFS_LAYOUT_ROOT_MAJOR    S[r * n + v]  (as tbfs_bfs_many)
+ *   TBFS_LAYOUT_VERTEX_MAJOR  S[v * k + r]
+ * Host or device outputs as opt->outputs_on_device; opt->mode AUTO picks
+ * push or pull per level, TOP_DOWN / BOTTOM_UP force one; opt->alpha is the
+ * push/pull threshold.  stats (may be NULL) receives k records; td_levels /
+ * bu_levels count the batch's push / pull levels and device_ms is the time
+ * of the launch that computed the root. */
+#define TBFS_LAYOUT_ROOT_MAJOR 0
+#define TBFS_LAYOUT_VERTEX_MAJOR 1
+#define TBFS_BATCH_MAX_ROOTS 256
+tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
+                           const tbfs_options *opt, int32_t layout, int32_t *S,
+                           int64_t *sigma, tbfs_stats *stats);
+
 /* One BFS that allocates nothing.  No counterpart in the reference: it is
  * for callers that must not have a library call cudaMalloc or cudaFree --
  * code running under a host framework that owns all device memory through

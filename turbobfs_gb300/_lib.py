@@ -27,6 +27,9 @@ STATUS_NAMES = {
 GRAPH_SYMMETRIC = 0x1
 GRAPH_DEVICE_PTRS = 0x2
 GRAPH_KEEP_ORDER = 0x4
+LAYOUT_ROOT_MAJOR = 0
+LAYOUT_VERTEX_MAJOR = 1
+BATCH_MAX_ROOTS = 256
 BUILD_SYMMETRIZE, BUILD_DROP_LOOPS, BUILD_DEDUP, BUILD_SORT = 0x1, 0x2, 0x4, 0x8
 
 
@@ -86,6 +89,8 @@ _SIGNATURES = {
     "tbfs_graph_last_stats": (c_int, [c_void_p, POINTER(Stats)]),
     "tbfs_bfs_many": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), _P_I32, _P_I64,
                               POINTER(Stats)]),
+    "tbfs_bfs_batch": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_int32, c_void_p,
+                               c_void_p, POINTER(Stats)]),
     "tbfs_bfs_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64,
                                  c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                  POINTER(Stats)]),

@@ -18,7 +18,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._lib import GRAPH_KEEP_ORDER, GRAPH_SYMMETRIC, Options, Stats, check, lib
+from ._lib import (GRAPH_KEEP_ORDER, GRAPH_SYMMETRIC, LAYOUT_ROOT_MAJOR, LAYOUT_VERTEX_MAJOR,
+                   Options, Stats, check, lib)
 
 MODES = {"auto": 0, "do": 0, "td": 1, "top_down": 1, "bu": 2, "bottom_up": 2}
 _P_I32 = ctypes.POINTER(ctypes.c_int32)
@@ -147,6 +148,23 @@ class Graph:
         check(lib().tbfs_bfs_many(self.handle, _ptr(roots, _P_I32), k, ctypes.byref(o),
                                   _ptr(S, _P_I32), _ptr(sg, _P_I64) if sg is not None else None,
                                   stats), "tbfs_bfs_many")
+        return S, sg, [stats[i].as_dict() for i in range(k)]
+
+    def bfs_batch(self, roots, mode="auto", sigma: bool = True, layout: str = "root", **kw):
+        """Frontier-matrix traversal from every root at once (256 per launch).
+        Returns (S, sigma, stats) like bfs_many; layout "root" gives k x n
+        arrays, "vertex" gives n x k."""
+        roots = _i32(roots)
+        k = int(roots.shape[0])
+        o = make_options(mode, sigma, **kw)
+        lay = LAYOUT_ROOT_MAJOR if layout == "root" else LAYOUT_VERTEX_MAJOR
+        shape = (k, self.n) if lay == LAYOUT_ROOT_MAJOR else (self.n, k)
+        S = np.empty(shape, dtype=np.int32)
+        sg = np.empty(shape, dtype=np.int64) if sigma else None
+        stats = (Stats * max(k, 1))()
+        check(lib().tbfs_bfs_batch(self.handle, _ptr(roots, _P_I32), k, ctypes.byref(o), lay,
+                                   S.ctypes.data, sg.ctypes.data if sg is not None else None,
+                                   stats), "tbfs_bfs_batch")
         return S, sg, [stats[i].as_dict() for i in range(k)]
 
     def close(self) -> None:

@@ -119,6 +119,7 @@ static void graph_free(tbfs_graph *g) {
   if (g->ctl_host) cudaFreeHost(g->ctl_host);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
+  tbfs::batch_ws_free(g->batch);
   cudaSetDevice(cur);
   delete g;
 }

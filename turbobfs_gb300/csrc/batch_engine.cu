@@ -1,0 +1,1043 @@
+/*
+ * batch_engine.cu -- frontier-matrix BFS: up to 256 roots on one graph
+ * advance level by level together in one persistent, cooperatively launched
+ * kernel, sharing every list read among the roots.
+ *
+ * The reference runs one root per call (TurboBFS_CSC_TD/bfsgputdcsc_sc.cu:
+ * 47-149 and its siblings); a caller with many roots -- the forward phase of
+ * betweenness centrality, which is what S and sigma are for -- pays a full
+ * traversal per root.  Here the roots are the columns of a frontier matrix:
+ * every vertex holds a row of W 32-bit words, bit r standing for root r.
+ *
+ *   seen[v]   roots that have reached v
+ *   F_d[v]    roots for which v is at depth d  (three rotating buffers)
+ *   S_int[v][r], sig_int[v][r]   depth and path count of v from root r,
+ *             written once, when r reaches v (rows of 32 W entries)
+ *
+ * Level d builds F_{d+1} = (OR of F_d over in-neighbours) & ~seen and, for
+ * every root r newly at v, sigma_r[v] = sum of sigma_r[u] over in-neighbours
+ * u with r in F_d[u] -- the same semiring step as the single-source engine,
+ * one bit-column per root.  Two schedules:
+ *
+ *   pull  every vertex not yet reached by all roots scans its in-list.  The
+ *         lanes of a vertex group (4 W lanes, lane l owning the 8 roots of
+ *         row byte l) each test one in-neighbour's frontier row against the
+ *         vertex's unseen mask; only rows that hit are staged in shared
+ *         memory, after which every lane adds the path counts of its own
+ *         roots from that neighbour's row (16-byte loads of the roots set).
+ *         A vertex with more than seg_len in-list entries (a hub) is split
+ *         into segments scanned by different groups; they combine with
+ *         atomicOr / atomicAdd and the last segment to arrive finishes the
+ *         vertex (fence + arrival counter).
+ *   push  for small frontiers: edge-balanced over the out-lists of the
+ *         queue of F_d, atomicOr of the new bits into F_{d+1}[v] (first
+ *         touch of v appends it to the next queue), then a pull of the path
+ *         counts over the in-lists of the new queue only.
+ *
+ * Direction rule per level: push while the frontier queue's out-edges times
+ * alpha are below the in-list entries of vertices not yet reached by every
+ * root (Beamer, Asanovic, Patterson, SC 2012, with the batch's unexplored
+ * edges).
+ *
+ * Path counts are exact in uint64; a sum reaching 2^63 sets the root's bit
+ * in ctl->ovf.  The fast path ORs the high words of the running sums; only
+ * when that shows a sum at or above 2^63 is the list rescanned with per-root
+ * checks, so that the flag names exactly the roots that overflowed.
+ *
+ * Memory model as in the single-source engine: rows and counts read with
+ * plain loads were all written before the last grid barrier; a hub's last
+ * segment reads the atomically combined row with ld.global.cg after a fence.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "tbfs_internal.h"
+
+namespace tbfs {
+namespace {
+
+using dev::FULL;
+using dev::grid_barrier;
+
+constexpr int kBlock = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr int kPushRounds = 8; /* 32-edge rounds per push work item     */
+constexpr int kChunk = 32;     /* vertices / queue entries per pull item */
+constexpr int kClear = 256;    /* queue entries per row-clearing item    */
+
+/* ---- row access ---------------------------------------------------------- */
+
+template <int W>
+__device__ __forceinline__ void load_row(const unsigned *p, unsigned (&r)[W]) {
+  if constexpr (W == 8) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(p);
+    const uint4 b = *reinterpret_cast<const uint4 *>(p + 4);
+    r[0] = a.x, r[1] = a.y, r[2] = a.z, r[3] = a.w, r[4] = b.x, r[5] = b.y, r[6] = b.z, r[7] = b.w;
+  } else if constexpr (W == 4) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(p);
+    r[0] = a.x, r[1] = a.y, r[2] = a.z, r[3] = a.w;
+  } else if constexpr (W == 2) {
+    const uint2 a = *reinterpret_cast<const uint2 *>(p);
+    r[0] = a.x, r[1] = a.y;
+  } else {
+    r[0] = *p;
+  }
+}
+
+/* the same through L2 (rows combined by atomics during the current phase) */
+template <int W>
+__device__ __forceinline__ void load_row_cg(const unsigned *p, unsigned (&r)[W]) {
+  if constexpr (W == 8) {
+    const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(p));
+    const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(p + 4));
+    r[0] = a.x, r[1] = a.y, r[2] = a.z, r[3] = a.w, r[4] = b.x, r[5] = b.y, r[6] = b.z, r[7] = b.w;
+  } else if constexpr (W == 4) {
+    const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(p));
+    r[0] = a.x, r[1] = a.y, r[2] = a.z, r[3] = a.w;
+  } else if constexpr (W == 2) {
+    const uint2 a = __ldcg(reinterpret_cast<const uint2 *>(p));
+    r[0] = a.x, r[1] = a.y;
+  } else {
+    r[0] = __ldcg(p);
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void store_row(unsigned *p, const unsigned (&r)[W]) {
+  if constexpr (W == 8) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(r[0], r[1], r[2], r[3]);
+    *reinterpret_cast<uint4 *>(p + 4) = make_uint4(r[4], r[5], r[6], r[7]);
+  } else if constexpr (W == 4) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(r[0], r[1], r[2], r[3]);
+  } else if constexpr (W == 2) {
+    *reinterpret_cast<uint2 *>(p) = make_uint2(r[0], r[1]);
+  } else {
+    *p = r[0];
+  }
+}
+
+/* a[i] for a run-time i without dynamic register indexing */
+template <int W>
+__device__ __forceinline__ unsigned pick(const unsigned (&a)[W], int i) {
+  unsigned x = a[0];
+#pragma unroll
+  for (int w = 1; w < W; ++w)
+    if (i == w) x = a[w];
+  return x;
+}
+
+/* Lanes of one vertex group: 4 W lanes, lane gl owning the roots of byte gl
+ * of the row (roots 8 gl .. 8 gl + 7). */
+template <int W>
+struct Grp {
+  static constexpr int G = 4 * W;
+  static constexpr int PER_WARP = 32 / G;
+  int lane, gid, gl, gbase, wsel, sh;
+  unsigned gmask;
+  __device__ __forceinline__ Grp() {
+    lane = threadIdx.x & 31;
+    gid = lane / G;
+    gl = lane % G;
+    gbase = gid * G;
+    gmask = G == 32 ? FULL : (((1u << G) - 1u) << gbase);
+    wsel = gl >> 2;
+    sh = (gl & 3) * 8;
+  }
+};
+
+template <int W>
+__device__ __forceinline__ void group_or(unsigned (&x)[W], unsigned gmask) {
+#pragma unroll
+  for (int o = 1; o < 4 * W; o <<= 1)
+#pragma unroll
+    for (int w = 0; w < W; ++w) x[w] |= __shfl_xor_sync(gmask, x[w], o);
+}
+
+/* ---- path-count accumulation ---------------------------------------------- */
+
+template <bool EXACT>
+__device__ __forceinline__ void add1(unsigned long long &a, unsigned long long x, unsigned byte,
+                                     int b, unsigned &ovh, unsigned &ovm) {
+  if ((byte >> b) & 1u) {
+    a += x;
+    if (EXACT) {
+      if (a >> 63) ovm |= 1u << b;
+    } else {
+      ovh |= (unsigned)(a >> 32);
+    }
+  }
+}
+
+/* acc[b] += src[b] for every bit b of `byte` (src: the 8 counts of a row
+ * slice, 64-byte aligned).  Fast path: ovh collects the high words (bit 31
+ * set once any sum reached 2^63); EXACT: ovm gets the bit of every root
+ * whose sum reached 2^63. */
+template <bool EXACT>
+__device__ __forceinline__ void acc_bits(const unsigned long long *src, unsigned byte,
+                                         unsigned long long (&acc)[8], unsigned &ovh,
+                                         unsigned &ovm) {
+  if (byte & 0x0fu) {
+    const ulonglong2 x0 = *reinterpret_cast<const ulonglong2 *>(src);
+    const ulonglong2 x1 = *reinterpret_cast<const ulonglong2 *>(src + 2);
+    add1<EXACT>(acc[0], x0.x, byte, 0, ovh, ovm);
+    add1<EXACT>(acc[1], x0.y, byte, 1, ovh, ovm);
+    add1<EXACT>(acc[2], x1.x, byte, 2, ovh, ovm);
+    add1<EXACT>(acc[3], x1.y, byte, 3, ovh, ovm);
+  }
+  if (byte & 0xf0u) {
+    const ulonglong2 x2 = *reinterpret_cast<const ulonglong2 *>(src + 4);
+    const ulonglong2 x3 = *reinterpret_cast<const ulonglong2 *>(src + 6);
+    add1<EXACT>(acc[4], x2.x, byte, 4, ovh, ovm);
+    add1<EXACT>(acc[5], x2.y, byte, 5, ovh, ovm);
+    add1<EXACT>(acc[6], x3.x, byte, 6, ovh, ovm);
+    add1<EXACT>(acc[7], x3.y, byte, 7, ovh, ovm);
+  }
+}
+
+/* Scan in-list entries [lo, hi) of one vertex with its group.  found |= F_d[u]
+ * & want over the entries; with SIG, every lane adds to acc the path counts
+ * of its roots set in F_d[u] & want.  sm: the warp's 32 x W staging words. */
+template <int W, bool SIG, bool EXACT>
+__device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *Fd, int lo, int hi,
+                                          const unsigned (&want)[W], unsigned (&found)[W],
+                                          unsigned long long (&acc)[8], unsigned &ovh,
+                                          unsigned &ovm, unsigned *sm, const Grp<W> &g) {
+  constexpr int G = 4 * W;
+  constexpr int RS = 32 * W;
+  for (int base = lo; base < hi; base += G) {
+    const int i = base + g.gl;
+    const bool has = i < hi;
+    int u = 0;
+    unsigned m[W];
+    bool any = false;
+    if (has) {
+      u = __ldg(p.ic + i);
+      load_row<W>(Fd + (size_t)u * W, m);
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        m[w] &= want[w];
+        any |= m[w] != 0u;
+      }
+    } else {
+#pragma unroll
+      for (int w = 0; w < W; ++w) m[w] = 0u;
+    }
+#pragma unroll
+    for (int w = 0; w < W; ++w) found[w] |= m[w];
+    if (SIG) {
+      unsigned hits = __ballot_sync(g.gmask, any);
+      if (hits) {
+        if (any) store_row<W>(sm + g.lane * W, m);
+        __syncwarp(g.gmask);
+        hits >>= g.gbase;
+        do {
+          const int j = __ffs(hits) - 1;
+          hits &= hits - 1u;
+          const int uj = __shfl_sync(g.gmask, u, g.gbase + j);
+          const unsigned byte = (sm[(g.gbase + j) * W + g.wsel] >> g.sh) & 0xffu;
+          if (byte) acc_bits<EXACT>(p.sig_int + (size_t)uj * RS + 8 * g.gl, byte, acc, ovh, ovm);
+        } while (hits);
+        __syncwarp(g.gmask);
+      }
+    }
+  }
+}
+
+/* Per-root overflow bits of this lane's roots for the sums over [lo, hi):
+ * the slow, exact rescan, run only when the fast path saw a high bit. */
+template <int W>
+__device__ __forceinline__ unsigned exact_overflow(const BatchParams &p, const unsigned *Fd, int lo,
+                                                   int hi, const unsigned (&want)[W], unsigned *sm,
+                                                   const Grp<W> &g) {
+  unsigned f[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) f[w] = 0u;
+  unsigned long long a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned oh = 0, om = 0;
+  scan_list<W, true, true>(p, Fd, lo, hi, want, f, a, oh, om, sm, g);
+  return om;
+}
+
+/* write depth d+1 (and the counts) of the roots in byte nb of vertex v */
+template <int W, bool SIG>
+__device__ __forceinline__ void write_new(const BatchParams &p, int d, int v, unsigned nb,
+                                          const unsigned long long (&acc)[8], const Grp<W> &g) {
+  constexpr int RS = 32 * W;
+  if (!nb) return;
+  int *srow = p.S_int + (size_t)v * RS + 8 * g.gl;
+#pragma unroll
+  for (int b = 0; b < 8; ++b)
+    if ((nb >> b) & 1u) srow[b] = d + 1;
+  if (SIG) {
+    unsigned long long *crow = p.sig_int + (size_t)v * RS + 8 * g.gl;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+      if ((nb >> b) & 1u) crow[b] = acc[b];
+  }
+}
+
+template <int W>
+__device__ __forceinline__ bool row_full(const BatchParams &p, const unsigned (&a)[W],
+                                         const unsigned (&b)[W]) {
+  bool f = true;
+#pragma unroll
+  for (int w = 0; w < W; ++w) f &= (a[w] | b[w]) == p.valid[w];
+  return f;
+}
+
+/* ---- per-vertex work ------------------------------------------------------- */
+
+/* pull level, whole in-list of v (not a hub): discover and count */
+template <int W, bool SIG>
+__device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, int lo, int hi,
+                                            const unsigned (&sn)[W], const unsigned *Fd,
+                                            unsigned *F1, unsigned *sm, const Grp<W> &g,
+                                            bool &take, bool &full) {
+  unsigned want[W], found[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    want[w] = p.valid[w] & ~sn[w];
+    found[w] = 0u;
+  }
+  unsigned long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned ovh = 0, ovm = 0;
+  scan_list<W, SIG, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
+  bool anyf = false;
+#pragma unroll
+  for (int w = 0; w < W; ++w) anyf |= found[w] != 0u;
+  take = false;
+  full = false;
+  if (!__any_sync(g.gmask, anyf)) return;
+  group_or<W>(found, g.gmask);
+  if (SIG && __any_sync(g.gmask, (ovh >> 31) != 0u)) {
+    ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
+    if (ovm) atomicOr(&p.ctl->ovf[g.wsel], ovm << g.sh);
+  }
+  write_new<W, SIG>(p, d, v, (pick<W>(found, g.wsel) >> g.sh) & 0xffu, acc, g);
+  if (g.gl < W) {
+    const unsigned fw = pick<W>(found, g.gl);
+    if (fw) {
+      F1[(size_t)v * W + g.gl] = fw;
+      p.seen[(size_t)v * W + g.gl] = pick<W>(sn, g.gl) | fw;
+    }
+  }
+  take = true;
+  full = row_full<W>(p, sn, found);
+}
+
+/* Fold a segment's partial result into hub h: new bits into F1 (pull only),
+ * partial counts into sig_int by atomics.  found must be group-reduced. */
+template <int W, bool SIG, bool DISC>
+__device__ __forceinline__ void commit_segment(const BatchParams &p, int h, const unsigned (&found)[W],
+                                               const unsigned long long (&acc)[8], unsigned ovh,
+                                               const unsigned *Fd, int lo, int hi,
+                                               const unsigned (&want)[W], unsigned *F1,
+                                               unsigned *sm, const Grp<W> &g) {
+  constexpr int RS = 32 * W;
+  if (DISC && g.gl < W) {
+    const unsigned fw = pick<W>(found, g.gl);
+    if (fw) atomicOr(&F1[(size_t)h * W + g.gl], fw);
+  }
+  if (SIG) {
+    unsigned ovm = 0;
+    if (__any_sync(g.gmask, (ovh >> 31) != 0u)) ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
+    const unsigned nb = (pick<W>(found, g.wsel) >> g.sh) & 0xffu;
+    if (nb) {
+      unsigned long long *crow = p.sig_int + (size_t)h * RS + 8 * g.gl;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        if ((nb >> b) & 1u) {
+          const unsigned long long old = atomicAdd(crow + b, acc[b]);
+          const unsigned long long s = old + acc[b];
+          if (s < old || (s >> 63)) ovm |= 1u << b;
+        }
+      }
+    }
+    if (ovm) atomicOr(&p.ctl->ovf[g.wsel], ovm << g.sh);
+  }
+}
+
+/* arrival of one segment of hub h; true on the group of the last one */
+template <int W>
+__device__ __forceinline__ bool arrive_last(const BatchParams &p, int h, unsigned nseg,
+                                            const Grp<W> &g) {
+  __threadfence();
+  __syncwarp(g.gmask);
+  unsigned last = 0;
+  if (g.gl == 0) {
+    const unsigned old = atomicAdd(&p.seg_arrive[h], 1u);
+    last = ((old + 1u) % nseg) == 0u ? 1u : 0u;
+  }
+  last = __shfl_sync(g.gmask, last, g.gbase);
+  if (last) __threadfence();
+  return last != 0u;
+}
+
+/* pull level, one segment of hub h */
+template <int W, bool SIG>
+__device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h, int lo, int hi,
+                                             unsigned nseg, const unsigned (&sn)[W],
+                                             const unsigned *Fd, unsigned *F1, unsigned *sm,
+                                             const Grp<W> &g, bool &take, bool &full) {
+  unsigned want[W], found[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    want[w] = p.valid[w] & ~sn[w];
+    found[w] = 0u;
+  }
+  unsigned long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned ovh = 0, ovm = 0;
+  scan_list<W, SIG, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
+  bool anyf = false;
+#pragma unroll
+  for (int w = 0; w < W; ++w) anyf |= found[w] != 0u;
+  if (__any_sync(g.gmask, anyf)) {
+    group_or<W>(found, g.gmask);
+    commit_segment<W, SIG, true>(p, h, found, acc, ovh, Fd, lo, hi, want, F1, sm, g);
+  }
+  take = false;
+  full = false;
+  if (!arrive_last<W>(p, h, nseg, g)) return;
+  unsigned nx[W];
+  load_row_cg<W>(F1 + (size_t)h * W, nx);
+  bool anyn = false;
+#pragma unroll
+  for (int w = 0; w < W; ++w) anyn |= nx[w] != 0u;
+  if (!anyn) return;
+  unsigned long long none[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  write_new<W, false>(p, d, h, (pick<W>(nx, g.wsel) >> g.sh) & 0xffu, none, g);
+  if (g.gl < W) {
+    const unsigned fw = pick<W>(nx, g.gl);
+    if (fw) p.seen[(size_t)h * W + g.gl] = pick<W>(sn, g.gl) | fw;
+  }
+  take = true;
+  full = row_full<W>(p, sn, nx);
+}
+
+/* push level, second phase: counts of the roots new at v (all of them known
+ * now in F1[v]); finishes v (depths, seen, queue-membership bit) */
+template <int W, bool SIG>
+__device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v, int lo, int hi,
+                                             const unsigned *Fd, const unsigned *F1, unsigned *sm,
+                                             const Grp<W> &g, bool &full) {
+  unsigned want[W], sn[W];
+  load_row<W>(F1 + (size_t)v * W, want);
+  load_row<W>(p.seen + (size_t)v * W, sn);
+  unsigned long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (SIG) {
+    unsigned found[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) found[w] = 0u;
+    unsigned ovh = 0, ovm = 0;
+    scan_list<W, true, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
+    if (__any_sync(g.gmask, (ovh >> 31) != 0u)) {
+      ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
+      if (ovm) atomicOr(&p.ctl->ovf[g.wsel], ovm << g.sh);
+    }
+  }
+  write_new<W, SIG>(p, d, v, (pick<W>(want, g.wsel) >> g.sh) & 0xffu, acc, g);
+  if (g.gl < W) {
+    const unsigned ww = pick<W>(want, g.gl);
+    if (ww) p.seen[(size_t)v * W + g.gl] = pick<W>(sn, g.gl) | ww;
+  }
+  if (g.gl == 0) atomicAnd(&p.touched[v >> 5], ~(1u << (v & 31)));
+  full = row_full<W>(p, sn, want);
+}
+
+/* push level, second phase, one segment of hub h (path counts only) */
+template <int W>
+__device__ __forceinline__ void count_segment(const BatchParams &p, int d, int h, int lo, int hi,
+                                              unsigned nseg, const unsigned *Fd, unsigned *F1,
+                                              unsigned *sm, const Grp<W> &g, bool &full) {
+  unsigned want[W], found[W];
+  load_row<W>(F1 + (size_t)h * W, want);
+#pragma unroll
+  for (int w = 0; w < W; ++w) found[w] = 0u;
+  unsigned long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned ovh = 0, ovm = 0;
+  scan_list<W, true, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
+  bool anyf = false;
+#pragma unroll
+  for (int w = 0; w < W; ++w) anyf |= found[w] != 0u;
+  if (__any_sync(g.gmask, anyf)) {
+    group_or<W>(found, g.gmask);
+    commit_segment<W, true, false>(p, h, found, acc, ovh, Fd, lo, hi, want, F1, sm, g);
+  }
+  full = false;
+  if (!arrive_last<W>(p, h, nseg, g)) return;
+  unsigned sn[W];
+  load_row<W>(p.seen + (size_t)h * W, sn);
+  unsigned long long none[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  write_new<W, false>(p, d, h, (pick<W>(want, g.wsel) >> g.sh) & 0xffu, none, g);
+  if (g.gl < W) {
+    const unsigned ww = pick<W>(want, g.gl);
+    if (ww) p.seen[(size_t)h * W + g.gl] = pick<W>(sn, g.gl) | ww;
+  }
+  if (g.gl == 0) atomicAnd(&p.touched[h >> 5], ~(1u << (h & 31)));
+  full = row_full<W>(p, sn, want);
+}
+
+/* ---- queues ------------------------------------------------------------------ */
+
+/* Append, for every lane with take set, (v, out-degree dg) to a queue: one
+ * 64-bit atomic per warp reserves (count << 32 | edge sum), so e[] stays the
+ * exclusive prefix of out-degrees in queue order.  All 32 lanes call. */
+__device__ __forceinline__ void warp_enqueue(bool take, int v, unsigned dg, int *q, unsigned *e,
+                                             unsigned long long *ctr) {
+  const int lane = threadIdx.x & 31;
+  const unsigned bal = __ballot_sync(FULL, take);
+  if (!bal) return;
+  const unsigned mine = take ? dg : 0u;
+  unsigned inc = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const unsigned tot = __shfl_sync(FULL, inc, 31);
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(ctr, ((unsigned long long)__popc(bal) << 32) | tot);
+  base = __shfl_sync(FULL, base, 0);
+  if (take) {
+    const unsigned pos = (unsigned)(base >> 32) + __popc(bal & ((1u << lane) - 1u));
+    q[pos] = v;
+    e[pos] = (unsigned)base + inc - mine;
+  }
+}
+
+__device__ __forceinline__ unsigned nsegs(int deg, int seg_len) {
+  return (unsigned)((deg + seg_len - 1) / seg_len);
+}
+
+/* largest i < cnt with pre[i] <= t (pre nondecreasing, pre[0] = 0) */
+template <class T>
+__device__ __forceinline__ unsigned upper_owner(const T *pre, unsigned cnt, unsigned t) {
+  unsigned lo = 0, hi = cnt;
+  while (hi - lo > 1) {
+    const unsigned mid = (lo + hi) >> 1;
+    if ((unsigned)__ldcg(pre + mid) <= t)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+/* ---- the kernel ------------------------------------------------------------- */
+
+template <int W, bool SIG>
+__global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) {
+  constexpr int PER = Grp<W>::PER_WARP;
+  constexpr int RS = 32 * W;
+  __shared__ __align__(16) unsigned s_m[kWarps][32 * W];
+  __shared__ int s_bv[kWarps][32];
+  __shared__ unsigned s_bd[kWarps][32];
+  const Grp<W> g;
+  const int wid = threadIdx.x >> 5;
+  unsigned *sm = s_m[wid];
+  BatchCtl *ctl = p.ctl;
+  const long long tid = (long long)blockIdx.x * kBlock + threadIdx.x;
+  const long long nth = (long long)gridDim.x * kBlock;
+  const int n = p.n;
+
+  /* clear the rows and per-vertex words; zero the hubs' count rows (they are
+   * summed into by atomics) */
+  const long long rows = (long long)n * W;
+  for (long long i = tid; i < rows; i += nth) {
+    p.seen[i] = 0u;
+    p.F[0][i] = 0u;
+    p.F[1][i] = 0u;
+    p.F[2][i] = 0u;
+  }
+  for (long long i = tid; i < ((long long)n + 31) / 32; i += nth) p.touched[i] = 0u;
+  for (long long i = tid; i < n; i += nth) p.seg_arrive[i] = 0u;
+  if (SIG)
+    for (long long i = tid; i < (long long)p.nhub * RS; i += nth)
+      p.sig_int[(size_t)__ldg(p.hubs + i / RS) * RS + i % RS] = 0ull;
+  if (!grid_barrier(ctl, p.timeout_ns, -1)) return;
+
+  /* roots (k <= 256 = kBlock): CTA 0 sets their bits, depth 0, count 1, and
+   * builds Q_0 from the distinct root vertices */
+  if (blockIdx.x == 0) {
+    __shared__ int s_rv[kBlock];
+    const int t = threadIdx.x;
+    int v = 0;
+    if (t < p.k) {
+      v = __ldg(p.roots + t);
+      if (p.inv) v = __ldg(p.inv + v);
+      atomicOr(&p.seen[(size_t)v * W + (t >> 5)], 1u << (t & 31));
+      atomicOr(&p.F[0][(size_t)v * W + (t >> 5)], 1u << (t & 31));
+      p.S_int[(size_t)v * RS + t] = 0;
+      if (SIG) p.sig_int[(size_t)v * RS + t] = 1ull;
+    }
+    s_rv[t] = v;
+    __syncthreads();
+    bool first = t < p.k;
+    for (int j = 0; j < t && first; ++j)
+      if (s_rv[j] == v) first = false;
+    const unsigned dg = first ? (unsigned)(__ldg(p.rp + v + 1) - __ldg(p.rp + v)) : 0u;
+    const unsigned one = first ? 1u : 0u;
+    /* inclusive scans of the first-occurrence flags and of the degrees */
+    __shared__ unsigned s_cnt[kBlock], s_deg[kBlock];
+    s_cnt[t] = one;
+    s_deg[t] = dg;
+    __syncthreads();
+    for (int o = 1; o < kBlock; o <<= 1) {
+      const unsigned c = t >= o ? s_cnt[t - o] : 0u;
+      const unsigned e = t >= o ? s_deg[t - o] : 0u;
+      __syncthreads();
+      s_cnt[t] += c;
+      s_deg[t] += e;
+      __syncthreads();
+    }
+    if (first) {
+      const unsigned pos = s_cnt[t] - 1u;
+      p.q[0][pos] = v;
+      p.e[0][pos] = s_deg[t] - dg;
+    }
+    if (t == kBlock - 1) ctl->qctr[0] = ((unsigned long long)s_cnt[t] << 32) | s_deg[t];
+  }
+  if (!grid_barrier(ctl, p.timeout_ns, -1)) return;
+
+  unsigned ph = 0;            /* phase counter: work slot ph % 4 */
+  unsigned long long md = 0;  /* this lane's newly finished in-list entries  */
+  long long m_done = 0;       /* in-list entries of vertices every root reached,
+                                 summed from the per-level slots (identical in
+                                 every thread, so every CTA takes the same
+                                 direction) */
+
+  auto claim = [&](void) -> unsigned {
+    unsigned it = 0;
+    if (g.lane == 0) it = atomicAdd(&ctl->work[ph & 3u], 1u);
+    return __shfl_sync(FULL, it, 0);
+  };
+  /* entries finished during level d go to slot (d + 1) % 4, read at the
+   * start of level d + 1 */
+  auto flush_md = [&](int d) {
+    unsigned long long x = md;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+    if (g.lane == 0 && x) atomicAdd(&ctl->m_lvl[(d + 1) & 3], x);
+    md = 0;
+  };
+
+  for (int d = 0;; ++d) {
+    const unsigned long long qv = __ldcg(&ctl->qctr[d & 3]);
+    const unsigned qn = (unsigned)(qv >> 32), qe = (unsigned)qv;
+    if (qn == 0) break;
+    const unsigned qn_prev = d > 0 ? (unsigned)(__ldcg(&ctl->qctr[(d + 3) & 3]) >> 32) : 0u;
+    m_done += (long long)__ldcg(&ctl->m_lvl[d & 3]);
+    const long long m_unseen = p.nnz_in - m_done;
+    bool push;
+    if (p.mode == TBFS_MODE_TOP_DOWN)
+      push = true;
+    else if (p.mode == TBFS_MODE_BOTTOM_UP)
+      push = false;
+    else
+      push = (double)qe * (double)p.alpha < (double)m_unseen;
+    if (tid == 0) {
+      ctl->qctr[(d + 2) & 3] = 0ull;
+      ctl->hctr[(d + 2) & 3] = 0ull;
+      ctl->m_lvl[(d + 2) & 3] = 0ull;
+      ctl->levels = d + 1;
+      if (push)
+        ctl->push_levels += 1;
+      else
+        ctl->pull_levels += 1;
+    }
+    const int b0 = d % 3, b1 = (d + 1) % 3, bm = (d + 2) % 3;
+    const unsigned *Fd = p.F[b0];
+    unsigned *F1 = p.F[b1];
+    unsigned *Fm = p.F[bm];
+    unsigned long long *qctr1 = &ctl->qctr[(d + 1) & 3];
+    const unsigned nclear = (qn_prev + kClear - 1) / kClear;
+
+    /* clear the rows of F_{d-1} (buffer of F_{d+2}) listed in Q_{d-1} */
+    auto clear_item = [&](unsigned c) {
+      for (unsigned j = g.lane; j < (unsigned)kClear; j += 32) {
+        const unsigned idx = c * kClear + j;
+        if (idx < qn_prev) {
+          const int v = __ldcg(p.q[bm] + idx);
+          unsigned z[W];
+#pragma unroll
+          for (int w = 0; w < W; ++w) z[w] = 0u;
+          store_row<W>(Fm + (size_t)v * W, z);
+        }
+      }
+    };
+
+    if (push) {
+      /* ---- phase 1: discovery over the out-edges of Q_d ---- */
+      const unsigned nA = (qe + kPushRounds * 32 - 1) / (kPushRounds * 32);
+      if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+      for (;;) {
+        const unsigned it = claim();
+        if (it >= nA + nclear) break;
+        if (it >= nA) {
+          clear_item(it - nA);
+          continue;
+        }
+        for (int r = 0; r < kPushRounds; ++r) {
+          const unsigned t = it * (kPushRounds * 32) + r * 32 + g.lane;
+          bool first = false;
+          int v = 0;
+          unsigned dgo = 0;
+          if (t < qe) {
+            const unsigned o = upper_owner(p.e[b0], qn, t);
+            const int u = __ldcg(p.q[b0] + o);
+            v = __ldg(p.jr + __ldg(p.rp + u) + (int)(t - __ldcg(p.e[b0] + o)));
+            unsigned fr[W], sv[W];
+            load_row<W>(Fd + (size_t)u * W, fr);
+            load_row<W>(p.seen + (size_t)v * W, sv);
+            bool any = false;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+              const unsigned m = fr[w] & ~sv[w];
+              if (m) {
+                atomicOr(&F1[(size_t)v * W + w], m);
+                any = true;
+              }
+            }
+            if (any) {
+              const unsigned bit = 1u << (v & 31);
+              first = (atomicOr(&p.touched[v >> 5], bit) & bit) == 0u;
+              if (first) {
+                dgo = (unsigned)(__ldg(p.rp + v + 1) - __ldg(p.rp + v));
+                if (SIG) {
+                  const int indeg = __ldg(p.cp + v + 1) - __ldg(p.cp + v);
+                  if (indeg > p.seg_len) {
+                    const unsigned long long old = atomicAdd(
+                        &ctl->hctr[(d + 1) & 3],
+                        (1ull << 32) | (unsigned long long)nsegs(indeg, p.seg_len));
+                    p.hq[b1][old >> 32] = v;
+                    p.he[b1][old >> 32] = (unsigned)old;
+                  }
+                }
+              }
+            }
+          }
+          warp_enqueue(first, v, dgo, p.q[b1], p.e[b1], qctr1);
+        }
+      }
+      if (!grid_barrier(ctl, p.timeout_ns, d)) return;
+      ++ph;
+
+      /* ---- phase 2: path counts of the new vertices, finish them ---- */
+      const unsigned qn1 = (unsigned)(__ldcg(qctr1) >> 32);
+      const unsigned long long hv = SIG ? __ldcg(&ctl->hctr[(d + 1) & 3]) : 0ull;
+      const unsigned hn1 = (unsigned)(hv >> 32), hsegs = (unsigned)hv;
+      const unsigned nA2 = (qn1 + kChunk - 1) / kChunk;
+      const unsigned nB2 = (hsegs + PER - 1) / PER;
+      if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+      for (;;) {
+        const unsigned it = claim();
+        if (it >= nA2 + nB2) break;
+        if (it < nA2) {
+          for (int j = g.gid; j < kChunk; j += PER) {
+            const unsigned idx = it * kChunk + j;
+            bool full = false;
+            int deg = 0;
+            if (idx < qn1) {
+              const int v = __ldcg(p.q[b1] + idx);
+              const int lo = __ldg(p.cp + v), hi = __ldg(p.cp + v + 1);
+              deg = hi - lo;
+              if (!SIG || deg <= p.seg_len) count_vertex<W, SIG>(p, d, v, lo, hi, Fd, F1, sm, g, full);
+            }
+            if (g.gl == 0 && full) md += (unsigned long long)deg;
+          }
+        } else if constexpr (SIG) {
+          const unsigned s = (it - nA2) * PER + g.gid;
+          bool full = false;
+          int deg = 0;
+          if (s < hsegs) {
+            const unsigned i = upper_owner(p.he[b1], hn1, s);
+            const int h = __ldcg(p.hq[b1] + i);
+            const unsigned si = s - __ldcg(p.he[b1] + i);
+            const int cl = __ldg(p.cp + h), ch = __ldg(p.cp + h + 1);
+            deg = ch - cl;
+            const int lo = cl + (int)si * p.seg_len;
+            const int hi = min(ch, lo + p.seg_len);
+            count_segment<W>(p, d, h, lo, hi, nsegs(deg, p.seg_len), Fd, F1, sm, g, full);
+          }
+          if (g.gl == 0 && full) md += (unsigned long long)deg;
+        }
+      }
+      flush_md(d);
+      if (!grid_barrier(ctl, p.timeout_ns, d)) return;
+      ++ph;
+    } else {
+      /* ---- pull: every vertex not reached by all roots ---- */
+      const unsigned nA = ((unsigned)p.hub_segs + PER - 1) / PER;
+      const unsigned nB = ((unsigned)n + kChunk - 1) / kChunk;
+      if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+      for (;;) {
+        const unsigned it = claim();
+        if (it >= nA + nB + nclear) break;
+        if (it >= nA + nB) {
+          clear_item(it - nA - nB);
+          continue;
+        }
+        unsigned bcnt = 0;
+        const int steps = it < nA ? 1 : kChunk / PER; /* hub item: one segment per group */
+        for (int st = 0; st < steps; ++st) {
+          const int j = st * PER + g.gid;
+          bool take = false, full = false;
+          int v = 0, deg = 0;
+          if (it < nA) {
+            const unsigned s = it * PER + g.gid;
+            if (s < (unsigned)p.hub_segs) {
+              const unsigned i = upper_owner(p.hub_seg, (unsigned)p.nhub, s);
+              v = __ldg(p.hubs + i);
+              const unsigned si = s - (unsigned)__ldg(p.hub_seg + i);
+              const int cl = __ldg(p.cp + v), ch = __ldg(p.cp + v + 1);
+              deg = ch - cl;
+              unsigned sn[W];
+              load_row<W>(p.seen + (size_t)v * W, sn);
+              bool done = true;
+#pragma unroll
+              for (int w = 0; w < W; ++w) done &= sn[w] == p.valid[w];
+              if (!done) {
+                const int lo = cl + (int)si * p.seg_len;
+                const int hi = min(ch, lo + p.seg_len);
+                pull_segment<W, SIG>(p, d, v, lo, hi, nsegs(deg, p.seg_len), sn, Fd, F1, sm, g,
+                                     take, full);
+              }
+            }
+          } else {
+            v = (int)((it - nA) * kChunk) + j;
+            if (v < n) {
+              const int lo = __ldg(p.cp + v), hi = __ldg(p.cp + v + 1);
+              deg = hi - lo;
+              if (deg <= p.seg_len) {
+                unsigned sn[W];
+                load_row<W>(p.seen + (size_t)v * W, sn);
+                bool done = true;
+#pragma unroll
+                for (int w = 0; w < W; ++w) done &= sn[w] == p.valid[w];
+                if (!done) pull_vertex<W, SIG>(p, d, v, lo, hi, sn, Fd, F1, sm, g, take, full);
+              }
+            }
+          }
+          const bool tk = g.gl == 0 && take;
+          if (g.gl == 0 && full) md += (unsigned long long)deg;
+          const unsigned bal = __ballot_sync(FULL, tk);
+          if (tk) {
+            const unsigned pos = bcnt + __popc(bal & ((1u << g.lane) - 1u));
+            s_bv[wid][pos] = v;
+            s_bd[wid][pos] = (unsigned)(__ldg(p.rp + v + 1) - __ldg(p.rp + v));
+          }
+          bcnt += __popc(bal);
+        }
+        __syncwarp();
+        const bool tk = g.lane < (int)bcnt;
+        warp_enqueue(tk, tk ? s_bv[wid][g.lane] : 0, tk ? s_bd[wid][g.lane] : 0u, p.q[b1], p.e[b1],
+                     qctr1);
+        __syncwarp();
+      }
+      flush_md(d);
+      if (!grid_barrier(ctl, p.timeout_ns, d)) return;
+      ++ph;
+    }
+  }
+}
+
+/* ---- results: internal rows -> caller layout, per-root statistics ---------- */
+
+template <int W, bool SIG>
+__global__ void __launch_bounds__(256) fm_output_kernel(const BatchOutParams o) {
+  constexpr int RS = 32 * W;
+  __shared__ int sS[32][33];
+  __shared__ unsigned long long sG[SIG ? 32 : 1][33];
+  __shared__ unsigned long long s_vis[8][32], s_edg[8][32];
+  __shared__ int s_md[8][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int rb = blockIdx.y;
+  const int r = rb * 32 + lane;
+  const bool rv = r < o.k;
+  unsigned long long vis = 0, edg = 0;
+  int mdep = -1;
+  const int ntiles = (o.n + 31) / 32;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int i0 = tile * 32;
+    for (int j = wid; j < 32; j += 8) {
+      const int i = i0 + j;
+      int s = -1;
+      unsigned long long cv = 0;
+      if (i < o.n) {
+        const int v = o.inv ? __ldg(o.inv + i) : i;
+        const unsigned sw = __ldg(o.seen + (size_t)v * W + rb);
+        if (rv && ((sw >> lane) & 1u)) {
+          s = __ldg(o.S_int + (size_t)v * RS + r);
+          if (SIG) cv = __ldg(o.sig_int + (size_t)v * RS + r);
+          ++vis;
+          edg += (unsigned long long)(__ldg(o.rp + v + 1) - __ldg(o.rp + v));
+          mdep = max(mdep, s);
+        }
+        if (o.layout == TBFS_LAYOUT_VERTEX_MAJOR && rv) {
+          o.S_out[(size_t)i * o.ldo + r] = s;
+          if (SIG && o.sig_out) o.sig_out[(size_t)i * o.ldo + r] = cv;
+        }
+      }
+      if (o.layout == TBFS_LAYOUT_ROOT_MAJOR) {
+        sS[lane][j] = s;
+        if (SIG) sG[lane][j] = cv;
+      }
+    }
+    if (o.layout == TBFS_LAYOUT_ROOT_MAJOR) {
+      __syncthreads();
+      for (int rr = wid; rr < 32; rr += 8) {
+        const int root = rb * 32 + rr;
+        if (root < o.k && i0 + lane < o.n) {
+          o.S_out[(size_t)root * o.ldo + i0 + lane] = sS[rr][lane];
+          if (SIG && o.sig_out) o.sig_out[(size_t)root * o.ldo + i0 + lane] = sG[rr][lane];
+        }
+      }
+      __syncthreads();
+    }
+  }
+  s_vis[wid][lane] = vis;
+  s_edg[wid][lane] = edg;
+  s_md[wid][lane] = mdep;
+  __syncthreads();
+  if (wid == 0 && rv) {
+    unsigned long long a = 0, b = 0;
+    int m = -1;
+    for (int w = 0; w < 8; ++w) {
+      a += s_vis[w][lane];
+      b += s_edg[w][lane];
+      m = max(m, s_md[w][lane]);
+    }
+    if (a) {
+      atomicAdd(o.r_visited + r, a);
+      atomicAdd(o.r_edges + r, b);
+      atomicMax(o.r_maxd + r, m);
+    }
+  }
+}
+
+/* ---- hub list ------------------------------------------------------------------ */
+
+__global__ void hub_flag_kernel(const int *cp, int n, int seg_len, int *flag) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = (cp[i + 1] - cp[i]) > seg_len ? 1 : 0;
+  if (i == n) flag[n] = 0;
+}
+
+__global__ void hub_fill_kernel(const int *cp, int n, int seg_len, const int *pos, int *hubs,
+                                int *nseg) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (pos[i + 1] != pos[i]) {
+    hubs[pos[i]] = (int)i;
+    nseg[pos[i]] = (int)nsegs(cp[i + 1] - cp[i], seg_len);
+  }
+}
+
+template <int W, bool SIG>
+const void *kernel_of() {
+  return reinterpret_cast<const void *>(fm_bfs_kernel<W, SIG>);
+}
+
+const void *batch_kernel(int W, bool sigma) {
+  switch (W) {
+    case 1: return sigma ? kernel_of<1, true>() : kernel_of<1, false>();
+    case 2: return sigma ? kernel_of<2, true>() : kernel_of<2, false>();
+    case 4: return sigma ? kernel_of<4, true>() : kernel_of<4, false>();
+    case 8: return sigma ? kernel_of<8, true>() : kernel_of<8, false>();
+    default: return nullptr;
+  }
+}
+
+}  // namespace
+
+cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_seg, int *nhub,
+                       int *hub_segs, cudaStream_t s) {
+  *hubs = nullptr;
+  *hub_seg = nullptr;
+  *nhub = 0;
+  *hub_segs = 0;
+  int *pos = nullptr;
+  cudaError_t e = cudaMalloc(&pos, ((size_t)n + 1) * sizeof(int));
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)(((long long)n + 1 + 255) / 256);
+  hub_flag_kernel<<<blocks, 256, 0, s>>>(cp, n, seg_len, pos);
+  if ((e = cudaGetLastError()) == cudaSuccess) e = exclusive_scan(pos, (long long)n + 1, pos, s);
+  int cnt = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&cnt, pos + n, sizeof(int), cudaMemcpyDeviceToHost);
+  int *h = nullptr, *ns = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&h, ((size_t)cnt + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&ns, ((size_t)cnt + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(ns, 0, ((size_t)cnt + 1) * sizeof(int), s);
+  if (e == cudaSuccess && cnt > 0) {
+    hub_fill_kernel<<<(unsigned)(((long long)n + 255) / 256), 256, 0, s>>>(cp, n, seg_len, pos, h,
+                                                                           ns);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = exclusive_scan(ns, (long long)cnt + 1, ns, s);
+  int tot = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&tot, ns + cnt, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(pos);
+  if (e != cudaSuccess) {
+    cudaFree(h);
+    cudaFree(ns);
+    return e;
+  }
+  *hubs = h;
+  *hub_seg = ns;
+  *nhub = cnt;
+  *hub_segs = tot;
+  return cudaSuccess;
+}
+
+cudaError_t batch_geometry(int device, int W, bool sigma, LaunchGeom *out) {
+  const void *k = batch_kernel(W, sigma);
+  if (!k) return cudaErrorInvalidValue;
+  int sms = 0, coop = 0, per = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (e != cudaSuccess) return e;
+  if (!coop) return cudaErrorNotSupported;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, 0);
+  if (e != cudaSuccess) return e;
+  if (per < 1) return cudaErrorInvalidConfiguration;
+  out->block = kBlock;
+  out->grid = sms * per;
+  return cudaSuccess;
+}
+
+cudaError_t batch_launch(const BatchParams &p, int W, bool sigma, const LaunchGeom &g,
+                         cudaStream_t s) {
+  const void *k = batch_kernel(W, sigma);
+  if (!k) return cudaErrorInvalidValue;
+  void *args[] = {const_cast<BatchParams *>(&p)};
+  return cudaLaunchCooperativeKernel(k, dim3(g.grid), dim3(g.block), args, 0, s);
+}
+
+cudaError_t batch_output(const BatchOutParams &o, bool sigma, cudaStream_t s) {
+  const int ntiles = (o.n + 31) / 32;
+  const dim3 grid((unsigned)min(ntiles, 4096), (unsigned)((o.k + 31) / 32));
+  switch (o.W) {
+    case 1:
+      sigma ? fm_output_kernel<1, true><<<grid, 256, 0, s>>>(o)
+            : fm_output_kernel<1, false><<<grid, 256, 0, s>>>(o);
+      break;
+    case 2:
+      sigma ? fm_output_kernel<2, true><<<grid, 256, 0, s>>>(o)
+            : fm_output_kernel<2, false><<<grid, 256, 0, s>>>(o);
+      break;
+    case 4:
+      sigma ? fm_output_kernel<4, true><<<grid, 256, 0, s>>>(o)
+            : fm_output_kernel<4, false><<<grid, 256, 0, s>>>(o);
+      break;
+    case 8:
+      sigma ? fm_output_kernel<8, true><<<grid, 256, 0, s>>>(o)
+            : fm_output_kernel<8, false><<<grid, 256, 0, s>>>(o);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tbfs

@@ -57,6 +57,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "device_common.cuh"
 #include "tbfs_internal.h"
 
 #ifndef TBFS_EPT
@@ -72,7 +73,12 @@
 namespace tbfs {
 namespace {
 
-constexpr unsigned FULL = 0xffffffffu;
+using dev::FULL;
+using dev::add_chk;
+using dev::smem_add64;
+using dev::global_ns;
+using dev::grid_barrier;
+using dev::warp_find_owner;
 constexpr int kBlock = TBFS_BLOCK;
 constexpr int kWarps = kBlock / 32;
 constexpr int kWin = 128;          /* queue entries staged per warp window */
@@ -93,93 +99,6 @@ struct WarpWin {
   int a[kWin];                  /* list index of its first window edge      */
   unsigned s[kWin + 1];         /* window-relative start of its edges       */
 };
-
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ int ld_volatile(const int *p) {
-  return *reinterpret_cast<const volatile int *>(p);
-}
-
-/* a + b in uint64; flags sums that reach 2^63 or wrap */
-__device__ __forceinline__ unsigned long long add_chk(unsigned long long a,
-                                                      unsigned long long b, bool &ovf) {
-  const unsigned long long s = a + b;
-  if (s < a || (s >> 63)) ovf = true;
-  return s;
-}
-
-/* *acc += x for a 64-bit accumulator in shared memory, with two native
- * 32-bit atomics: the low word's returned old value yields the carry, which
- * is folded into the high word's add; the high word's returned old value
- * detects sums reaching 2^63.  Exact modulo 2^64 under any interleaving. */
-__device__ __forceinline__ void smem_add64(unsigned long long *acc, unsigned long long x,
-                                           bool &ovf) {
-  unsigned *w = reinterpret_cast<unsigned *>(acc);
-  const unsigned xl = (unsigned)x, xh = (unsigned)(x >> 32);
-  const unsigned old_l = atomicAdd(w, xl);
-  const unsigned carry = (old_l + xl) < old_l ? 1u : 0u;
-  const unsigned add_h = xh + carry;
-  const unsigned old_h = atomicAdd(w + 1, add_h);
-  const unsigned new_h = old_h + add_h;
-  if (new_h < old_h || (new_h >> 31) || add_h < xh) ovf = true;
-}
-
-/* Grid-wide barrier.  Thread 0 of every CTA arrives on a counter; the last
- * one resets it and bumps the generation word.  Every wait is bounded by
- * timeout_ns of wall time (globaltimer): on expiry the CTA records
- * TBFS_ERR_TIMEOUT and returns false, and so does every CTA that sees the
- * error word set, so the kernel always terminates. */
-__device__ bool grid_barrier(BfsCtl *ctl, long long timeout_ns, int level) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned gen = ld_acquire_u32(&ctl->bar_gen);
-    __threadfence();
-    const unsigned prev = atomicAdd(&ctl->bar_arrive, 1u);
-    if (prev == gridDim.x - 1) {
-      atomicExch(&ctl->bar_arrive, 0u);
-      __threadfence();
-      st_release_u32(&ctl->bar_gen, gen + 1);
-    } else {
-      const unsigned long long t0 = global_ns();
-      unsigned spins = 0;
-      while (ld_acquire_u32(&ctl->bar_gen) == gen) {
-        if ((++spins & 31u) == 0) {
-          if (ld_volatile(&ctl->status) != 0) {
-            ok = 0;
-            break;
-          }
-          if ((long long)(global_ns() - t0) > timeout_ns) {
-            atomicCAS(&ctl->status, 0, (int)TBFS_ERR_TIMEOUT);
-            atomicCAS(&ctl->timeout_level, 0, level + 2);
-            ok = 0;
-            break;
-          }
-        }
-      }
-    }
-    __threadfence();
-    if (ld_volatile(&ctl->status) != 0) ok = 0;
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
 
 /* Append, for every lane, the entries j < N with bit j of `take` set to the
  * next level's queue (q, e, a): one 64-bit atomic per warp reserves
@@ -227,26 +146,6 @@ __device__ __forceinline__ void warp_append(unsigned take, const int (&vv)[N],
   }
 }
 
-/* Largest i in [0, qn) with e[i] <= target (e nondecreasing, e[0] = 0).
- * 32-ary search: each step narrows the range 32x with one load per lane. */
-__device__ __forceinline__ unsigned warp_find_owner(const int *e, unsigned qn, unsigned target) {
-  const int lane = threadIdx.x & 31;
-  unsigned lo = 0, hi = qn;
-  while (hi - lo > 32) {
-    const unsigned step = (hi - lo + 31) / 32;
-    const unsigned pidx = lo + lane * step;
-    const bool pred = pidx < hi && (unsigned)__ldcg(e + pidx) <= target;
-    const unsigned m = __ballot_sync(FULL, pred);
-    const unsigned last = 31 - __clz(m);
-    lo = lo + last * step;
-    const unsigned nhi = lo + step;
-    hi = nhi < hi ? nhi : hi;
-  }
-  const unsigned pidx = lo + lane;
-  const bool pred = pidx < hi && (unsigned)__ldcg(e + pidx) <= target;
-  const unsigned m = __ballot_sync(FULL, pred);
-  return lo + (31 - __clz(m));
-}
 
 /* A level's queue: entries i < qn with vertex q[i], edge offset e[i], list
  * start a[i]; qe is the total of its out-degrees. */

@@ -166,8 +166,8 @@ int grid_for(long long work) {
 
 }  // namespace
 
-/* exclusive scan over len ints, in place allowed */
-static cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t s) {
+/* exclusive scan over len ints, in place allowed; synchronises the stream */
+cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t s) {
   const long long tiles = (len + kScanTile - 1) / kScanTile;
   if (tiles == 0) return cudaSuccess;
   int *partial = nullptr;

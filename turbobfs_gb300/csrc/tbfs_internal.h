@@ -81,12 +81,94 @@ struct LaunchGeom {
 cudaError_t bfs_launch(const BfsParams &p, const LaunchGeom &g, cudaStream_t s);
 cudaError_t bfs_geometry(int device, LaunchGeom *out);
 
+/* ---- frontier-matrix batch (batch_engine.cu) ----
+ * Up to 256 roots on one graph advance together: bit r of a vertex's row
+ * stands for root r.  Rows are W 32-bit words (W in {1, 2, 4, 8}, 32 W >=
+ * roots of the launch); per-root values are rows of 32 W entries. */
+constexpr int kBatchMaxRoots = 256;
+
+struct __align__(128) BatchCtl {
+  unsigned long long qctr[4]; /* Q_d: (count << 32) | out-edge sum, slot d % 4   */
+  unsigned long long hctr[4]; /* hub part of Q_d: (count << 32) | segments       */
+  unsigned long long m_lvl[4]; /* in-list entries of vertices all roots reached
+                                  during level d - 1, slot d % 4              */
+  unsigned work[4];           /* dynamic work counter of phase ph in work[ph % 4] */
+  int status, timeout_level;
+  int levels, push_levels, pull_levels;
+  int pad0;
+  unsigned ovf[8]; /* bit r: a path count of root r reached 2^63 */
+  unsigned pad1[2];
+  unsigned bar_arrive;
+  unsigned pad2[31];
+  unsigned bar_gen;
+  unsigned pad3[31];
+};
+
+struct BatchParams {
+  const int *cp, *ic; /* in-lists (pull)  */
+  const int *rp, *jr; /* out-lists (push) */
+  int n;
+  long long nnz_in;   /* in-list entries (direction rule) */
+  int k;              /* roots of this launch (<= 256)      */
+  const int *roots;   /* root r: caller vertex id (k)       */
+  const int *inv;     /* caller id -> internal id, or null  */
+  unsigned *seen;     /* [n][W]: roots that reached v       */
+  unsigned *F[3];     /* [n][W]: F_d in F[d % 3]            */
+  int *q[3];          /* frontier queue of level d in q[d % 3] ...      */
+  unsigned *e[3];     /* ... with the exclusive prefix of out-degrees   */
+  int *hq[3];         /* hub entries of the queue (vertex) ...          */
+  unsigned *he[3];    /* ... with the exclusive prefix of segment counts */
+  unsigned *touched;  /* [ceil(n/32)] queue membership during push levels */
+  unsigned *seg_arrive; /* [n] cumulative segment arrivals (hubs)         */
+  int *S_int;         /* [n][32W] depth of v from root r (valid where seen) */
+  unsigned long long *sig_int; /* [n][32W] path counts, or null            */
+  const int *hubs;    /* vertices with more than seg_len in-list entries   */
+  const int *hub_seg; /* exclusive prefix of their segment counts (nhub+1) */
+  int nhub;
+  int hub_segs;
+  int seg_len;
+  BatchCtl *ctl;
+  long long timeout_ns;
+  float alpha;
+  int mode;           /* TBFS_MODE_*: AUTO, TOP_DOWN (push), BOTTOM_UP (pull) */
+  unsigned valid[8];  /* root bits in use, per word */
+};
+
+struct BatchOutParams {
+  int n, k, W, layout;
+  long long ldo;      /* output row stride: n (root-major) or the caller's k */
+  const int *inv;     /* caller id -> internal id, or null */
+  const int *rp;      /* out-degrees for the per-root edge counts */
+  const unsigned *seen;
+  const int *S_int;
+  const unsigned long long *sig_int;
+  int *S_out;                  /* root r, caller id i at r * ldo + i (root-major)
+                                  or i * ldo + r (vertex-major) */
+  unsigned long long *sig_out; /* same layout, or null        */
+  unsigned long long *r_visited, *r_edges; /* per-root stats (k) */
+  int *r_maxd;
+};
+
+/* Graph-wide hub list for segment length seg_len: hubs (nhub) and hub_seg
+ * (nhub + 1, exclusive prefix of ceil(indeg / seg_len)), allocated here. */
+cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_seg, int *nhub,
+                       int *hub_segs, cudaStream_t s);
+cudaError_t batch_geometry(int device, int W, bool sigma, LaunchGeom *out);
+cudaError_t batch_launch(const BatchParams &p, int W, bool sigma, const LaunchGeom &g,
+                         cudaStream_t s);
+cudaError_t batch_output(const BatchOutParams &o, bool sigma, cudaStream_t s);
+
+struct BatchWS; /* per-graph batch workspace (batch_api.cu) */
+void batch_ws_free(BatchWS *ws);
+
 /* graph ingest helpers (graph_ingest.cu) */
 cudaError_t validate_csc(const int *cp, const int *ic, int n, long long nnz,
                          int *d_flag, cudaStream_t s);
 cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
                                 int n, int *ptr_out, int *idx_out, int *d_flag,
                                 cudaStream_t s);
+/* exclusive prefix sum of len ints (in place allowed); synchronises s */
+cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t s);
 cudaError_t expand_columns(const int *cp, int n, int *col_of_entry, cudaStream_t s);
 /* Degree-based grouping of the vertices (see graph_ingest.cu).  On return
  * *identity tells whether the order is unchanged (then perm/inv/cp2/ic2 are
@@ -125,6 +207,7 @@ struct tbfs_graph {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t last_stream = nullptr;
   tbfs::LaunchGeom geom;
+  tbfs::BatchWS *batch = nullptr; /* frontier-matrix workspace, on first use */
   bool pending = false; /* a traversal was enqueued and not yet collected */
   tbfs_stats last = {};
 };
