@@ -69,6 +69,31 @@ class BfsResult:
     stats: dict = field(default_factory=dict)
 
 
+def _trace_buffer(o: Options, trace: int):
+    if not trace:
+        return None
+    tr = np.zeros((max(int(trace), 2), 4), dtype=np.int64)
+    o.level_trace = tr.ctypes.data_as(_P_I64)
+    o.level_trace_cap = tr.shape[0]
+    return tr
+
+
+def _parse_trace(tr: np.ndarray):
+    """Per-level records {level, start_us, vertices, edges, direction} with
+    start_us relative to the first level, and the end time."""
+    t0 = tr[0, 0]
+    recs, end = [], None
+    for d, (t, qn, qe, dr) in enumerate(tr.tolist()):
+        if dr == -1:
+            end = (t - t0) / 1e3
+            break
+        if t == 0:
+            break
+        recs.append({"level": d, "start_us": (t - t0) / 1e3, "vertices": qn,
+                     "edges": qe, "direction": "bu" if dr == 1 else "td"})
+    return recs, end
+
+
 class Graph:
     """A graph resident in GPU memory until ``close()``."""
 
@@ -114,28 +139,14 @@ class Graph:
         o = make_options(mode, sigma, **kw)
         S = np.empty(self.n, dtype=np.int32)
         sg = np.empty(self.n, dtype=np.int64) if sigma else None
-        tr = None
-        if trace:
-            tr = np.zeros((max(int(trace), 2), 4), dtype=np.int64)
-            o.level_trace = tr.ctypes.data_as(_P_I64)
-            o.level_trace_cap = tr.shape[0]
+        tr = _trace_buffer(o, trace)
         st = Stats()
         check(lib().tbfs_bfs(self.handle, int(root), ctypes.byref(o), _ptr(S, _P_I32),
                              _ptr(sg, _P_I64) if sg is not None else None, ctypes.byref(st)),
               "tbfs_bfs")
         stats = st.as_dict()
         if tr is not None:
-            t0 = tr[0, 0]
-            recs, end = [], None
-            for d, (t, qn, qe, dr) in enumerate(tr.tolist()):
-                if dr == -1:
-                    end = (t - t0) / 1e3
-                    break
-                if t == 0:
-                    break
-                recs.append({"level": d, "start_us": (t - t0) / 1e3, "vertices": qn,
-                             "edges": qe, "direction": "bu" if dr == 1 else "td"})
-            stats["trace"], stats["trace_end_us"] = recs, end
+            stats["trace"], stats["trace_end_us"] = _parse_trace(tr)
         return BfsResult(S, sg, stats)
 
     def bfs_many(self, roots, mode="auto", sigma: bool = True, **kw):
@@ -150,13 +161,16 @@ class Graph:
                                   stats), "tbfs_bfs_many")
         return S, sg, [stats[i].as_dict() for i in range(k)]
 
-    def bfs_batch(self, roots, mode="auto", sigma: bool = True, layout: str = "root", **kw):
+    def bfs_batch(self, roots, mode="auto", sigma: bool = True, layout: str = "root",
+                  trace: int = 0, **kw):
         """Frontier-matrix traversal from every root at once (256 per launch).
         Returns (S, sigma, stats) like bfs_many; layout "root" gives k x n
-        arrays, "vertex" gives n x k."""
+        arrays, "vertex" gives n x k.  trace=k records the levels of the first
+        launch in stats[0]["trace"] (push levels show as "td", pull as "bu")."""
         roots = _i32(roots)
         k = int(roots.shape[0])
         o = make_options(mode, sigma, **kw)
+        tr = _trace_buffer(o, trace)
         lay = LAYOUT_ROOT_MAJOR if layout == "root" else LAYOUT_VERTEX_MAJOR
         shape = (k, self.n) if lay == LAYOUT_ROOT_MAJOR else (self.n, k)
         S = np.empty(shape, dtype=np.int32)
@@ -165,7 +179,10 @@ class Graph:
         check(lib().tbfs_bfs_batch(self.handle, _ptr(roots, _P_I32), k, ctypes.byref(o), lay,
                                    S.ctypes.data, sg.ctypes.data if sg is not None else None,
                                    stats), "tbfs_bfs_batch")
-        return S, sg, [stats[i].as_dict() for i in range(k)]
+        out = [stats[i].as_dict() for i in range(k)]
+        if tr is not None and out:
+            out[0]["trace"], out[0]["trace_end_us"] = _parse_trace(tr)
+        return S, sg, out
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:

@@ -40,6 +40,8 @@ struct BatchWS {
   size_t stage_entries = 0;
   bool stage_sigma = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  long long *trace_dev = nullptr;
+  int trace_cap = 0;
 };
 
 tbfs_status fail(cudaError_t e, const char *what) {
@@ -102,7 +104,7 @@ tbfs_status ensure_ws(tbfs_graph *g, int W, bool sigma, cudaStream_t s) {
     TRY(cudaMalloc(&w->F, 3 * n * W * sizeof(unsigned)), "alloc rows");
     TRY(cudaMalloc(&w->S_int, n * rs * sizeof(int)), "alloc depth rows");
     if (keep_sigma) TRY(cudaMalloc(&w->sig_int, n * rs * sizeof(unsigned long long)), "alloc count rows");
-    w->seg_len = 256 * W;
+    w->seg_len = 128 * W; /* a hub segment is about one work item of the pull */
     TRY(batch_hubs(g->cp, g->n, w->seg_len, &w->hubs, &w->hub_seg, &w->nhub, &w->hub_segs, s),
         "hub list");
     w->W = W;
@@ -144,6 +146,7 @@ void batch_ws_free(BatchWS *w) {
   cudaFree(w->ctl);
   cudaFree(w->S_stage);
   cudaFree(w->sig_stage);
+  cudaFree(w->trace_dev);
   if (w->roots_host) cudaFreeHost(w->roots_host);
   if (w->rst_host) cudaFreeHost(w->rst_host);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -242,9 +245,28 @@ extern "C" tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32
     p.timeout_ns = timeout;
     p.alpha = o.alpha;
     p.mode = o.mode;
-    for (int i = 0; i < 8; ++i) {
-      const int lo = 32 * i;
-      p.valid[i] = kg >= lo + 32 ? 0xffffffffu : kg > lo ? ((1u << (kg - lo)) - 1u) : 0u;
+    /* level trace of the first launch (roots 0..255) */
+    const bool tracing = r0 == 0 && o.level_trace != nullptr && o.level_trace_cap >= 2;
+    if (tracing) {
+      if (w->trace_cap < o.level_trace_cap) {
+        cudaFree(w->trace_dev);
+        w->trace_dev = nullptr;
+        w->trace_cap = 0;
+        TRY(cudaMalloc(&w->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long)), "alloc trace");
+        w->trace_cap = o.level_trace_cap;
+      }
+      TRY(cudaMemsetAsync(w->trace_dev, 0, (size_t)o.level_trace_cap * 4 * sizeof(long long), s),
+          "clear trace");
+      p.trace = w->trace_dev;
+      p.trace_cap = o.level_trace_cap;
+    }
+    /* root r lives at bit 8 (c % G) + 2 (c / G) + (r & 1) of a row, c = r / 2,
+     * G = 4 W (lane-major order, see batch_engine.cu) */
+    for (int i = 0; i < 8; ++i) p.valid[i] = 0u;
+    for (int r = 0; r < kg; ++r) {
+      const int c = r >> 1, G = 4 * W;
+      const int b = 8 * (c % G) + 2 * (c / G) + (r & 1);
+      p.valid[b >> 5] |= 1u << (b & 31);
     }
 
     /* where the results go */
@@ -292,6 +314,10 @@ extern "C" tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32
         "read control block");
     TRY(cudaMemcpyAsync(w->rst_host, w->rst, tbfs::kStatBytes, cudaMemcpyDeviceToHost, s),
         "read stats");
+    if (tracing)
+      TRY(cudaMemcpyAsync(o.level_trace, w->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long),
+                          cudaMemcpyDeviceToHost, s),
+          "read trace");
     if (!o.outputs_on_device) {
       if (layout == TBFS_LAYOUT_ROOT_MAJOR) {
         TRY(cudaMemcpyAsync(S + (size_t)r0 * n, S_out, (size_t)kg * n * sizeof(int),

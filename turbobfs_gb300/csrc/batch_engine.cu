@@ -62,9 +62,15 @@ using dev::grid_barrier;
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-constexpr int kPushRounds = 8; /* 32-edge rounds per push work item     */
-constexpr int kChunk = 32;     /* vertices / queue entries per pull item */
-constexpr int kClear = 256;    /* queue entries per row-clearing item    */
+constexpr int kPushRounds = 8;    /* 32-edge rounds per push work item         */
+constexpr int kClear = 256;       /* queue entries per row-clearing item        */
+constexpr int kVCost = 4;         /* a vertex costs like this many list entries */
+constexpr long long kItemCost = 1024; /* list entries + vertex costs per item    */
+#ifndef TBFS_BATCH_HITS
+#define TBFS_BATCH_HITS 6
+#endif
+constexpr int kHitBatch = TBFS_BATCH_HITS; /* hit rows whose counts are fetched per round trip */
+constexpr int kStageU64 = kHitBatch * 32 * 8; /* per-warp stage: hits x lanes x 8 counts */
 
 /* ---- row access ---------------------------------------------------------- */
 
@@ -127,13 +133,18 @@ __device__ __forceinline__ unsigned pick(const unsigned (&a)[W], int i) {
   return x;
 }
 
-/* Lanes of one vertex group: 4 W lanes, lane gl owning the roots of byte gl
- * of the row (roots 8 gl .. 8 gl + 7). */
+/* Lanes of one vertex group: G = 4 W lanes for the 32 W roots of a row.
+ * Lane gl owns the root pairs c_q = gl + G q (q = 0..3), i.e. roots 2 c_q
+ * and 2 c_q + 1.  A pair is one 16-byte chunk of a path-count row, so the
+ * chunks of the G lanes for one q are contiguous: copies and stores of a
+ * group are coalesced, and each lane's staged chunks are conflict-free.
+ * Frontier rows store root r = 2 c_q + t at bit position 8 gl + 2 q + t
+ * (bit_of_root), so a lane's 8 roots are exactly byte gl of every row. */
 template <int W>
 struct Grp {
   static constexpr int G = 4 * W;
   static constexpr int PER_WARP = 32 / G;
-  int lane, gid, gl, gbase, wsel, sh;
+  int lane, gid, gl, gbase;
   unsigned gmask;
   __device__ __forceinline__ Grp() {
     lane = threadIdx.x & 31;
@@ -141,10 +152,28 @@ struct Grp {
     gl = lane % G;
     gbase = gid * G;
     gmask = G == 32 ? FULL : (((1u << G) - 1u) << gbase);
-    wsel = gl >> 2;
-    sh = (gl & 3) * 8;
   }
+  /* root of bit b of this lane's mask */
+  __device__ __forceinline__ int root(int b) const { return 2 * (gl + G * (b >> 1)) + (b & 1); }
 };
+
+/* bit position of root r in a frontier row of W words (see Grp) */
+__device__ __host__ __forceinline__ int bit_of_root(int r, int W) {
+  const int c = r >> 1, G = 4 * W;
+  return 8 * (c % G) + 2 * (c / G) + (r & 1);
+}
+
+/* this lane's 8-bit mask (its byte) of a row held in registers */
+template <int W>
+__device__ __forceinline__ unsigned lane_bits(const unsigned (&row)[W], const Grp<W> &g) {
+  return (pick<W>(row, g.gl >> 2) >> (8 * (g.gl & 3))) & 0xffu;
+}
+
+/* the same for a row in shared memory */
+template <int W>
+__device__ __forceinline__ unsigned lane_bits_smem(const unsigned *row, const Grp<W> &g) {
+  return (row[g.gl >> 2] >> (8 * (g.gl & 3))) & 0xffu;
+}
 
 template <int W>
 __device__ __forceinline__ void group_or(unsigned (&x)[W], unsigned gmask) {
@@ -154,12 +183,35 @@ __device__ __forceinline__ void group_or(unsigned (&x)[W], unsigned gmask) {
     for (int w = 0; w < W; ++w) x[w] |= __shfl_xor_sync(gmask, x[w], o);
 }
 
+/* Per-warp shared memory: m (32 x W words) stages the hit rows' masks;
+ * stage (kHitBatch x 4 x 32 lanes x 2 counts) receives the 16-byte chunks of
+ * path counts each lane fetches asynchronously for its own roots: chunk q of
+ * hit b of a lane at stage[((4 b + q) * 32 + lane) * 2]. */
+struct WarpSmem {
+  unsigned *m;
+  unsigned long long *stage;
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+#if TBFS_BATCH_CA
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+#else /* L2 only: the rows are gathered once per hit, L1 reuse is rare */
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+#endif
+}
+
+/* wait for this thread's outstanding cp.async copies */
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 /* ---- path-count accumulation ---------------------------------------------- */
 
 template <bool EXACT>
-__device__ __forceinline__ void add1(unsigned long long &a, unsigned long long x, unsigned byte,
+__device__ __forceinline__ void add1(unsigned long long &a, unsigned long long x, unsigned lm,
                                      int b, unsigned &ovh, unsigned &ovm) {
-  if ((byte >> b) & 1u) {
+  if ((lm >> b) & 1u) {
     a += x;
     if (EXACT) {
       if (a >> 63) ovm |= 1u << b;
@@ -169,29 +221,31 @@ __device__ __forceinline__ void add1(unsigned long long &a, unsigned long long x
   }
 }
 
-/* acc[b] += src[b] for every bit b of `byte` (src: the 8 counts of a row
- * slice, 64-byte aligned).  Fast path: ovh collects the high words (bit 31
- * set once any sum reached 2^63); EXACT: ovm gets the bit of every root
- * whose sum reached 2^63. */
+/* acc[b] += the staged count of bit b of lane mask lm (one hit).  Fast path:
+ * ovh collects the high words (bit 31 set once any sum reached 2^63); EXACT:
+ * ovm gets the bit of every root whose sum reached 2^63. */
 template <bool EXACT>
-__device__ __forceinline__ void acc_bits(const unsigned long long *src, unsigned byte,
-                                         unsigned long long (&acc)[8], unsigned &ovh,
-                                         unsigned &ovm) {
-  if (byte & 0x0fu) {
-    const ulonglong2 x0 = *reinterpret_cast<const ulonglong2 *>(src);
-    const ulonglong2 x1 = *reinterpret_cast<const ulonglong2 *>(src + 2);
-    add1<EXACT>(acc[0], x0.x, byte, 0, ovh, ovm);
-    add1<EXACT>(acc[1], x0.y, byte, 1, ovh, ovm);
-    add1<EXACT>(acc[2], x1.x, byte, 2, ovh, ovm);
-    add1<EXACT>(acc[3], x1.y, byte, 3, ovh, ovm);
+__device__ __forceinline__ void acc_staged(const unsigned long long *slot, unsigned lm,
+                                           unsigned long long (&acc)[8], unsigned &ovh,
+                                           unsigned &ovm) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if ((lm >> (2 * q)) & 3u) {
+      const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(slot + q * 64);
+      add1<EXACT>(acc[2 * q], x.x, lm, 2 * q, ovh, ovm);
+      add1<EXACT>(acc[2 * q + 1], x.y, lm, 2 * q + 1, ovh, ovm);
+    }
   }
-  if (byte & 0xf0u) {
-    const ulonglong2 x2 = *reinterpret_cast<const ulonglong2 *>(src + 4);
-    const ulonglong2 x3 = *reinterpret_cast<const ulonglong2 *>(src + 6);
-    add1<EXACT>(acc[4], x2.x, byte, 4, ovh, ovm);
-    add1<EXACT>(acc[5], x2.y, byte, 5, ovh, ovm);
-    add1<EXACT>(acc[6], x3.x, byte, 6, ovh, ovm);
-    add1<EXACT>(acc[7], x3.y, byte, 7, ovh, ovm);
+}
+
+/* record the overflow of the roots of lane mask ovm */
+template <int W>
+__device__ __forceinline__ void report_overflow(const BatchParams &p, unsigned ovm, const Grp<W> &g) {
+  while (ovm) {
+    const int b = __ffs(ovm) - 1;
+    ovm &= ovm - 1u;
+    const int r = g.root(b);
+    atomicOr(&p.ctl->ovf[r >> 5], 1u << (r & 31));
   }
 }
 
@@ -202,7 +256,7 @@ template <int W, bool SIG, bool EXACT>
 __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *Fd, int lo, int hi,
                                           const unsigned (&want)[W], unsigned (&found)[W],
                                           unsigned long long (&acc)[8], unsigned &ovh,
-                                          unsigned &ovm, unsigned *sm, const Grp<W> &g) {
+                                          unsigned &ovm, const WarpSmem &sm, const Grp<W> &g) {
   constexpr int G = 4 * W;
   constexpr int RS = 32 * W;
   for (int base = lo; base < hi; base += G) {
@@ -228,15 +282,35 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
     if (SIG) {
       unsigned hits = __ballot_sync(g.gmask, any);
       if (hits) {
-        if (any) store_row<W>(sm + g.lane * W, m);
+        if (any) store_row<W>(sm.m + g.lane * W, m);
         __syncwarp(g.gmask);
         hits >>= g.gbase;
+        /* kHitBatch hit rows per round trip: every lane copies the chunks of
+         * its roots that are set (16 bytes per root pair) into its own stage
+         * slots, waits for its own copies only, then accumulates */
+        unsigned long long *mine = sm.stage + g.lane * 2;
         do {
-          const int j = __ffs(hits) - 1;
-          hits &= hits - 1u;
-          const int uj = __shfl_sync(g.gmask, u, g.gbase + j);
-          const unsigned byte = (sm[(g.gbase + j) * W + g.wsel] >> g.sh) & 0xffu;
-          if (byte) acc_bits<EXACT>(p.sig_int + (size_t)uj * RS + 8 * g.gl, byte, acc, ovh, ovm);
+          unsigned lms[kHitBatch];
+#pragma unroll
+          for (int b = 0; b < kHitBatch; ++b) {
+            lms[b] = 0u;
+            if (hits) {
+              const int j = __ffs(hits) - 1;
+              hits &= hits - 1u;
+              const int uj = __shfl_sync(g.gmask, u, g.gbase + j);
+              const unsigned lm = lane_bits_smem<W>(sm.m + (g.gbase + j) * W, g);
+              lms[b] = lm;
+              const unsigned long long *row = p.sig_int + (size_t)uj * RS;
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if ((lm >> (2 * q)) & 3u)
+                  cp_async16(mine + (4 * b + q) * 64, row + 2 * (g.gl + G * q));
+            }
+          }
+          cp_async_wait_all();
+#pragma unroll
+          for (int b = 0; b < kHitBatch; ++b)
+            if (lms[b]) acc_staged<EXACT>(mine + 4 * b * 64, lms[b], acc, ovh, ovm);
         } while (hits);
         __syncwarp(g.gmask);
       }
@@ -248,7 +322,7 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
  * the slow, exact rescan, run only when the fast path saw a high bit. */
 template <int W>
 __device__ __forceinline__ unsigned exact_overflow(const BatchParams &p, const unsigned *Fd, int lo,
-                                                   int hi, const unsigned (&want)[W], unsigned *sm,
+                                                   int hi, const unsigned (&want)[W], const WarpSmem &sm,
                                                    const Grp<W> &g) {
   unsigned f[W];
 #pragma unroll
@@ -259,21 +333,27 @@ __device__ __forceinline__ unsigned exact_overflow(const BatchParams &p, const u
   return om;
 }
 
-/* write depth d+1 (and the counts) of the roots in byte nb of vertex v */
+/* write depth d+1 (and the counts) of the roots of lane mask nb at vertex v */
 template <int W, bool SIG>
 __device__ __forceinline__ void write_new(const BatchParams &p, int d, int v, unsigned nb,
                                           const unsigned long long (&acc)[8], const Grp<W> &g) {
   constexpr int RS = 32 * W;
+  constexpr int G = 4 * W;
   if (!nb) return;
-  int *srow = p.S_int + (size_t)v * RS + 8 * g.gl;
 #pragma unroll
-  for (int b = 0; b < 8; ++b)
-    if ((nb >> b) & 1u) srow[b] = d + 1;
-  if (SIG) {
-    unsigned long long *crow = p.sig_int + (size_t)v * RS + 8 * g.gl;
-#pragma unroll
-    for (int b = 0; b < 8; ++b)
-      if ((nb >> b) & 1u) crow[b] = acc[b];
+  for (int q = 0; q < 4; ++q) {
+    const unsigned pr = (nb >> (2 * q)) & 3u;
+    if (!pr) continue;
+    const size_t at = (size_t)v * RS + 2 * (g.gl + G * q);
+    if (pr == 3u) {
+      *reinterpret_cast<int2 *>(p.S_int + at) = make_int2(d + 1, d + 1);
+      if (SIG)
+        *reinterpret_cast<ulonglong2 *>(p.sig_int + at) = make_ulonglong2(acc[2 * q], acc[2 * q + 1]);
+    } else {
+      const int t = pr == 2u ? 1 : 0;
+      p.S_int[at + t] = d + 1;
+      if (SIG) p.sig_int[at + t] = t ? acc[2 * q + 1] : acc[2 * q];
+    }
   }
 }
 
@@ -292,7 +372,7 @@ __device__ __forceinline__ bool row_full(const BatchParams &p, const unsigned (&
 template <int W, bool SIG>
 __device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, int lo, int hi,
                                             const unsigned (&sn)[W], const unsigned *Fd,
-                                            unsigned *F1, unsigned *sm, const Grp<W> &g,
+                                            unsigned *F1, const WarpSmem &sm, const Grp<W> &g,
                                             bool &take, bool &full) {
   unsigned want[W], found[W];
 #pragma unroll
@@ -312,9 +392,9 @@ __device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, 
   group_or<W>(found, g.gmask);
   if (SIG && __any_sync(g.gmask, (ovh >> 31) != 0u)) {
     ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
-    if (ovm) atomicOr(&p.ctl->ovf[g.wsel], ovm << g.sh);
+    report_overflow<W>(p, ovm, g);
   }
-  write_new<W, SIG>(p, d, v, (pick<W>(found, g.wsel) >> g.sh) & 0xffu, acc, g);
+  write_new<W, SIG>(p, d, v, lane_bits<W>(found, g), acc, g);
   if (g.gl < W) {
     const unsigned fw = pick<W>(found, g.gl);
     if (fw) {
@@ -333,7 +413,7 @@ __device__ __forceinline__ void commit_segment(const BatchParams &p, int h, cons
                                                const unsigned long long (&acc)[8], unsigned ovh,
                                                const unsigned *Fd, int lo, int hi,
                                                const unsigned (&want)[W], unsigned *F1,
-                                               unsigned *sm, const Grp<W> &g) {
+                                               const WarpSmem &sm, const Grp<W> &g) {
   constexpr int RS = 32 * W;
   if (DISC && g.gl < W) {
     const unsigned fw = pick<W>(found, g.gl);
@@ -342,19 +422,19 @@ __device__ __forceinline__ void commit_segment(const BatchParams &p, int h, cons
   if (SIG) {
     unsigned ovm = 0;
     if (__any_sync(g.gmask, (ovh >> 31) != 0u)) ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
-    const unsigned nb = (pick<W>(found, g.wsel) >> g.sh) & 0xffu;
+    const unsigned nb = lane_bits<W>(found, g);
     if (nb) {
-      unsigned long long *crow = p.sig_int + (size_t)h * RS + 8 * g.gl;
+      unsigned long long *crow = p.sig_int + (size_t)h * RS;
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
         if ((nb >> b) & 1u) {
-          const unsigned long long old = atomicAdd(crow + b, acc[b]);
+          const unsigned long long old = atomicAdd(crow + g.root(b), acc[b]);
           const unsigned long long s = old + acc[b];
           if (s < old || (s >> 63)) ovm |= 1u << b;
         }
       }
     }
-    if (ovm) atomicOr(&p.ctl->ovf[g.wsel], ovm << g.sh);
+    report_overflow<W>(p, ovm, g);
   }
 }
 
@@ -378,7 +458,7 @@ __device__ __forceinline__ bool arrive_last(const BatchParams &p, int h, unsigne
 template <int W, bool SIG>
 __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h, int lo, int hi,
                                              unsigned nseg, const unsigned (&sn)[W],
-                                             const unsigned *Fd, unsigned *F1, unsigned *sm,
+                                             const unsigned *Fd, unsigned *F1, const WarpSmem &sm,
                                              const Grp<W> &g, bool &take, bool &full) {
   unsigned want[W], found[W];
 #pragma unroll
@@ -406,7 +486,7 @@ __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h,
   for (int w = 0; w < W; ++w) anyn |= nx[w] != 0u;
   if (!anyn) return;
   unsigned long long none[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  write_new<W, false>(p, d, h, (pick<W>(nx, g.wsel) >> g.sh) & 0xffu, none, g);
+  write_new<W, false>(p, d, h, lane_bits<W>(nx, g), none, g);
   if (g.gl < W) {
     const unsigned fw = pick<W>(nx, g.gl);
     if (fw) p.seen[(size_t)h * W + g.gl] = pick<W>(sn, g.gl) | fw;
@@ -419,7 +499,7 @@ __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h,
  * now in F1[v]); finishes v (depths, seen, queue-membership bit) */
 template <int W, bool SIG>
 __device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v, int lo, int hi,
-                                             const unsigned *Fd, const unsigned *F1, unsigned *sm,
+                                             const unsigned *Fd, const unsigned *F1, const WarpSmem &sm,
                                              const Grp<W> &g, bool &full) {
   unsigned want[W], sn[W];
   load_row<W>(F1 + (size_t)v * W, want);
@@ -433,10 +513,10 @@ __device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v,
     scan_list<W, true, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
     if (__any_sync(g.gmask, (ovh >> 31) != 0u)) {
       ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
-      if (ovm) atomicOr(&p.ctl->ovf[g.wsel], ovm << g.sh);
+      report_overflow<W>(p, ovm, g);
     }
   }
-  write_new<W, SIG>(p, d, v, (pick<W>(want, g.wsel) >> g.sh) & 0xffu, acc, g);
+  write_new<W, SIG>(p, d, v, lane_bits<W>(want, g), acc, g);
   if (g.gl < W) {
     const unsigned ww = pick<W>(want, g.gl);
     if (ww) p.seen[(size_t)v * W + g.gl] = pick<W>(sn, g.gl) | ww;
@@ -449,7 +529,7 @@ __device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v,
 template <int W>
 __device__ __forceinline__ void count_segment(const BatchParams &p, int d, int h, int lo, int hi,
                                               unsigned nseg, const unsigned *Fd, unsigned *F1,
-                                              unsigned *sm, const Grp<W> &g, bool &full) {
+                                              const WarpSmem &sm, const Grp<W> &g, bool &full) {
   unsigned want[W], found[W];
   load_row<W>(F1 + (size_t)h * W, want);
 #pragma unroll
@@ -469,7 +549,7 @@ __device__ __forceinline__ void count_segment(const BatchParams &p, int d, int h
   unsigned sn[W];
   load_row<W>(p.seen + (size_t)h * W, sn);
   unsigned long long none[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  write_new<W, false>(p, d, h, (pick<W>(want, g.wsel) >> g.sh) & 0xffu, none, g);
+  write_new<W, false>(p, d, h, lane_bits<W>(want, g), none, g);
   if (g.gl < W) {
     const unsigned ww = pick<W>(want, g.gl);
     if (ww) p.seen[(size_t)h * W + g.gl] = pick<W>(sn, g.gl) | ww;
@@ -510,6 +590,28 @@ __device__ __forceinline__ unsigned nsegs(int deg, int seg_len) {
   return (unsigned)((deg + seg_len - 1) / seg_len);
 }
 
+/* Smallest i in [0, cnt] with f(i) >= target, f nondecreasing on [0, cnt)
+ * and f(cnt) taken as +infinity; 32-ary search, all 32 lanes call with the
+ * same arguments. */
+template <class F>
+__device__ __forceinline__ unsigned warp_lower_bound(F f, unsigned cnt, long long target) {
+  const int lane = threadIdx.x & 31;
+  unsigned lo = 0, hi = cnt;
+  while (hi - lo > 32) {
+    const unsigned step = (hi - lo + 31) / 32;
+    const unsigned pidx = lo + lane * step;
+    const bool pred = pidx < hi && f(pidx) < target;
+    const unsigned c = __popc(__ballot_sync(FULL, pred));
+    if (c == 0) return lo;
+    const unsigned nhi = lo + c * step;
+    lo = lo + (c - 1) * step + 1;
+    hi = nhi < hi ? nhi : hi;
+  }
+  const unsigned pidx = lo + lane;
+  const bool pred = pidx < hi && f(pidx) < target;
+  return lo + __popc(__ballot_sync(FULL, pred));
+}
+
 /* largest i < cnt with pre[i] <= t (pre nondecreasing, pre[0] = 0) */
 template <class T>
 __device__ __forceinline__ unsigned upper_owner(const T *pre, unsigned cnt, unsigned t) {
@@ -535,7 +637,8 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
   __shared__ unsigned s_bd[kWarps][32];
   const Grp<W> g;
   const int wid = threadIdx.x >> 5;
-  unsigned *sm = s_m[wid];
+  extern __shared__ __align__(16) unsigned long long s_dyn[]; /* kWarps x kStageU64 with SIG */
+  const WarpSmem sm{s_m[wid], SIG ? s_dyn + (size_t)wid * kStageU64 : nullptr};
   BatchCtl *ctl = p.ctl;
   const long long tid = (long long)blockIdx.x * kBlock + threadIdx.x;
   const long long nth = (long long)gridDim.x * kBlock;
@@ -566,8 +669,9 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
     if (t < p.k) {
       v = __ldg(p.roots + t);
       if (p.inv) v = __ldg(p.inv + v);
-      atomicOr(&p.seen[(size_t)v * W + (t >> 5)], 1u << (t & 31));
-      atomicOr(&p.F[0][(size_t)v * W + (t >> 5)], 1u << (t & 31));
+      const int b = bit_of_root(t, W);
+      atomicOr(&p.seen[(size_t)v * W + (b >> 5)], 1u << (b & 31));
+      atomicOr(&p.F[0][(size_t)v * W + (b >> 5)], 1u << (b & 31));
       p.S_int[(size_t)v * RS + t] = 0;
       if (SIG) p.sig_int[(size_t)v * RS + t] = 1ull;
     }
@@ -636,6 +740,13 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
       push = false;
     else
       push = (double)qe * (double)p.alpha < (double)m_unseen;
+    if (tid == 0 && p.trace && d < p.trace_cap - 1) {
+      long long *rec = p.trace + 4 * (long long)d;
+      rec[0] = (long long)dev::global_ns();
+      rec[1] = qn;
+      rec[2] = qe;
+      rec[3] = push ? 0 : 1;
+    }
     if (tid == 0) {
       ctl->qctr[(d + 2) & 3] = 0ull;
       ctl->hctr[(d + 2) & 3] = 0ull;
@@ -727,18 +838,27 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
       const unsigned qn1 = (unsigned)(__ldcg(qctr1) >> 32);
       const unsigned long long hv = SIG ? __ldcg(&ctl->hctr[(d + 1) & 3]) : 0ull;
       const unsigned hn1 = (unsigned)(hv >> 32), hsegs = (unsigned)hv;
-      const unsigned nA2 = (qn1 + kChunk - 1) / kChunk;
+      const unsigned qe1 = (unsigned)__ldcg(qctr1);
+      const unsigned *e1 = p.e[b1];
+      /* items of ~kItemCost list entries + vertex costs over the queue */
+      const long long cost2 = (long long)qe1 + (long long)kVCost * qn1;
+      const unsigned nA2 = (unsigned)((cost2 + kItemCost - 1) / kItemCost);
       const unsigned nB2 = (hsegs + PER - 1) / PER;
+      auto qcost = [&](unsigned i) -> long long {
+        return (long long)__ldcg(e1 + i) + (long long)kVCost * i;
+      };
       if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
       for (;;) {
         const unsigned it = claim();
         if (it >= nA2 + nB2) break;
         if (it < nA2) {
-          for (int j = g.gid; j < kChunk; j += PER) {
-            const unsigned idx = it * kChunk + j;
+          const unsigned is = warp_lower_bound(qcost, qn1, (long long)it * kItemCost);
+          const unsigned ie = warp_lower_bound(qcost, qn1, (long long)(it + 1) * kItemCost);
+          for (unsigned base = is; base < ie; base += PER) {
+            const unsigned idx = base + g.gid;
             bool full = false;
             int deg = 0;
-            if (idx < qn1) {
+            if (idx < ie) {
               const int v = __ldcg(p.q[b1] + idx);
               const int lo = __ldg(p.cp + v), hi = __ldg(p.cp + v + 1);
               deg = hi - lo;
@@ -769,7 +889,11 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
     } else {
       /* ---- pull: every vertex not reached by all roots ---- */
       const unsigned nA = ((unsigned)p.hub_segs + PER - 1) / PER;
-      const unsigned nB = ((unsigned)n + kChunk - 1) / kChunk;
+      const long long cost = p.nnz_in + (long long)kVCost * n;
+      const unsigned nB = (unsigned)((cost + kItemCost - 1) / kItemCost);
+      auto vcost = [&](unsigned v) -> long long {
+        return (long long)__ldg(p.cp + v) + (long long)kVCost * v;
+      };
       if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
       for (;;) {
         const unsigned it = claim();
@@ -779,9 +903,14 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
           continue;
         }
         unsigned bcnt = 0;
-        const int steps = it < nA ? 1 : kChunk / PER; /* hub item: one segment per group */
-        for (int st = 0; st < steps; ++st) {
-          const int j = st * PER + g.gid;
+        /* hub item: one segment per group; vertex item: the vertices of
+         * ~kItemCost list entries + vertex costs, PER at a time */
+        unsigned vs = 0, ve = 1;
+        if (it >= nA) {
+          vs = warp_lower_bound(vcost, (unsigned)n, (long long)(it - nA) * kItemCost);
+          ve = warp_lower_bound(vcost, (unsigned)n, (long long)(it - nA + 1) * kItemCost);
+        }
+        for (unsigned base = vs; base < ve; base += (it < nA ? 1u : (unsigned)PER)) {
           bool take = false, full = false;
           int v = 0, deg = 0;
           if (it < nA) {
@@ -805,8 +934,9 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
               }
             }
           } else {
-            v = (int)((it - nA) * kChunk) + j;
-            if (v < n) {
+            const unsigned vv = base + g.gid;
+            v = (int)vv;
+            if (vv < ve) {
               const int lo = __ldg(p.cp + v), hi = __ldg(p.cp + v + 1);
               deg = hi - lo;
               if (deg <= p.seg_len) {
@@ -828,6 +958,14 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
             s_bd[wid][pos] = (unsigned)(__ldg(p.rp + v + 1) - __ldg(p.rp + v));
           }
           bcnt += __popc(bal);
+          if (bcnt > 32u - PER) { /* the buffer could overflow next step: flush */
+            __syncwarp();
+            const bool ft = g.lane < (int)bcnt;
+            warp_enqueue(ft, ft ? s_bv[wid][g.lane] : 0, ft ? s_bd[wid][g.lane] : 0u, p.q[b1],
+                         p.e[b1], qctr1);
+            __syncwarp();
+            bcnt = 0;
+          }
         }
         __syncwarp();
         const bool tk = g.lane < (int)bcnt;
@@ -839,6 +977,14 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
       if (!grid_barrier(ctl, p.timeout_ns, d)) return;
       ++ph;
     }
+  }
+  if (tid == 0 && p.trace) {
+    const int slot = ctl->levels < p.trace_cap - 1 ? ctl->levels : p.trace_cap - 1;
+    long long *rec = p.trace + 4 * (long long)slot;
+    rec[0] = (long long)dev::global_ns();
+    rec[1] = 0;
+    rec[2] = 0;
+    rec[3] = -1;
   }
 }
 
@@ -866,8 +1012,9 @@ __global__ void __launch_bounds__(256) fm_output_kernel(const BatchOutParams o) 
       unsigned long long cv = 0;
       if (i < o.n) {
         const int v = o.inv ? __ldg(o.inv + i) : i;
-        const unsigned sw = __ldg(o.seen + (size_t)v * W + rb);
-        if (rv && ((sw >> lane) & 1u)) {
+        const int rbit = bit_of_root(rv ? r : 0, W);
+        const unsigned sw = __ldg(o.seen + (size_t)v * W + (rbit >> 5));
+        if (rv && ((sw >> (rbit & 31)) & 1u)) {
           s = __ldg(o.S_int + (size_t)v * RS + r);
           if (SIG) cv = __ldg(o.sig_int + (size_t)v * RS + r);
           ++vis;
@@ -939,6 +1086,11 @@ const void *kernel_of() {
   return reinterpret_cast<const void *>(fm_bfs_kernel<W, SIG>);
 }
 
+/* dynamic shared memory of the kernel: the path-count stage */
+size_t stage_bytes(bool sigma) {
+  return sigma ? (size_t)kWarps * kStageU64 * sizeof(unsigned long long) : 0;
+}
+
 const void *batch_kernel(int W, bool sigma) {
   switch (W) {
     case 1: return sigma ? kernel_of<1, true>() : kernel_of<1, false>();
@@ -999,7 +1151,12 @@ cudaError_t batch_geometry(int device, int W, bool sigma, LaunchGeom *out) {
   e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   if (e != cudaSuccess) return e;
   if (!coop) return cudaErrorNotSupported;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, 0);
+  const size_t dyn = stage_bytes(sigma);
+  if (dyn) {
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+  }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kBlock, dyn);
   if (e != cudaSuccess) return e;
   if (per < 1) return cudaErrorInvalidConfiguration;
   out->block = kBlock;
@@ -1012,7 +1169,7 @@ cudaError_t batch_launch(const BatchParams &p, int W, bool sigma, const LaunchGe
   const void *k = batch_kernel(W, sigma);
   if (!k) return cudaErrorInvalidValue;
   void *args[] = {const_cast<BatchParams *>(&p)};
-  return cudaLaunchCooperativeKernel(k, dim3(g.grid), dim3(g.block), args, 0, s);
+  return cudaLaunchCooperativeKernel(k, dim3(g.grid), dim3(g.block), args, stage_bytes(sigma), s);
 }
 
 cudaError_t batch_output(const BatchOutParams &o, bool sigma, cudaStream_t s) {

@@ -132,6 +132,8 @@ struct BatchParams {
   float alpha;
   int mode;           /* TBFS_MODE_*: AUTO, TOP_DOWN (push), BOTTOM_UP (pull) */
   unsigned valid[8];  /* root bits in use, per word */
+  long long *trace;   /* trace_cap x 4 records {ns, |Q_d|, out-edges, 0 push / 1 pull}, or null */
+  int trace_cap;
 };
 
 struct BatchOutParams {
