@@ -151,6 +151,55 @@ tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
                            const tbfs_options *opt, int32_t layout, int32_t *S,
                            int64_t *sigma, tbfs_stats *stats);
 
+/* ---- many graphs, one root each: a packed arena ----
+ * No counterpart in the reference.  g graphs in one int32 offset arena:
+ * graph i has n[i] vertices and nnz[i] CSC entries; col_ptr holds the g
+ * column-pointer arrays one after another (n[i] + 1 entries each, 0-based
+ * within the graph) and row_idx the g row-index arrays (nnz[i] each).
+ * flags: TBFS_GRAPH_SYMMETRIC when every graph is undirected (in-lists
+ * double as out-lists); otherwise out-lists are built.  The arena keeps its
+ * vertex numbering.  tbfs_arena_bfs runs one BFS per graph from roots[i]
+ * (vertex of graph i), all graphs advancing together in one persistent
+ * launch (1024 at a time); S and sigma are packed like the arena (graph i at
+ * vertex offset n[0] + ... + n[i-1]) and stats gets g records.  Every
+ * traversal is top-down with exact int64 path counts. */
+typedef struct tbfs_arena tbfs_arena;
+tbfs_status tbfs_arena_create(int32_t g, const int32_t *n, const int64_t *nnz,
+                              const int32_t *col_ptr, const int32_t *row_idx,
+                              uint32_t flags, tbfs_arena **out);
+tbfs_status tbfs_arena_info(const tbfs_arena *a, int32_t *g, int64_t *vertices,
+                            int64_t *entries);
+tbfs_status tbfs_arena_bfs(tbfs_arena *a, const int32_t *roots, const tbfs_options *opt,
+                           int32_t *S, int64_t *sigma, tbfs_stats *stats);
+void tbfs_arena_destroy(tbfs_arena *a);
+
+/* ---- serving: a request loop with continuous batching ----
+ * No counterpart in the reference.  tbfs_server_create starts a host thread
+ * owning a device-memory pool of mem_budget bytes and max_slots (<= 1024)
+ * traversal slots on the current device.  tbfs_server_submit queues a query
+ * (resident graph g, root) whose results go to the caller's host arrays S[n]
+ * and sigma[n] (sigma NULL: depths only), which must stay valid until
+ * tbfs_server_wait(ticket) returns.  The loop admits queued queries into free
+ * slots while the pool has room (about 48 n bytes per query with path
+ * counts, 36 n without), runs one persistent launch that advances every
+ * admitted query level by level -- a few levels at a time while queries are
+ * waiting, so that they join soon, else to completion -- and retires the
+ * finished ones.  Results equal tbfs_bfs's for the same (graph, root)
+ * whatever else is running.  wait returns the query's status, statistics
+ * and latency (submit to results in host memory, ms).  The graphs must
+ * outlive their queries.  destroy fails queued queries, finishes running
+ * ones and stops the thread. */
+typedef struct tbfs_server tbfs_server;
+tbfs_status tbfs_server_create(int32_t max_slots, int64_t mem_budget, const tbfs_options *opt,
+                               tbfs_server **out);
+tbfs_status tbfs_server_submit(tbfs_server *s, tbfs_graph *g, int32_t root, int32_t *S,
+                               int64_t *sigma, uint64_t *ticket);
+tbfs_status tbfs_server_wait(tbfs_server *s, uint64_t ticket, tbfs_stats *stats,
+                             double *latency_ms);
+tbfs_status tbfs_server_counters(tbfs_server *s, int64_t *launches, int64_t *levels,
+                                 int64_t *completed);
+void tbfs_server_destroy(tbfs_server *s);
+
 /* One BFS that allocates nothing.  No counterpart in the reference: it is
  * for callers that must not have a library call cudaMalloc or cudaFree --
  * code running under a host framework that owns all device memory through

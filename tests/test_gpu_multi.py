@@ -1,0 +1,173 @@
+"""GPU parity of the multi-instance engine: packed arenas of many graphs
+(tbfs_arena_*) and the serving loop (tbfs_server_*).
+
+Bar: bit-exact.  Every traversal's S and sigma must equal the exact oracle
+(arena) or the single traversal tbfs_bfs of the same (graph, root) run
+alone (server: "the same alone and in the mix"), whatever else shares the
+launch, the memory budget or the admission order."""
+import threading
+
+import numpy as np
+import pytest
+
+import oracle
+import turbobfs_gb300 as tb
+from turbobfs_gb300 import graphs
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_graphs(count, seed, lo=6, hi=12):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        kind = i % 3
+        scale = int(rng.integers(lo, hi + 1))
+        if kind == 0:
+            n = 1 << scale
+            out.append(graphs.erdos_renyi(n, 4 * n, seed=seed + i))
+        elif kind == 1:
+            out.append(graphs.rmat(scale, 8, seed=seed + i))
+        else:
+            out.append(graphs.grid(max(2, int(2 ** (scale / 2))), seed=seed + i))
+    return out
+
+
+def _check_exact(h, r, S, sg, st):
+    eS, esg, ovf, levels = oracle.exact_bfs(h.col_ptr, h.row_idx, int(r))
+    assert np.array_equal(S, eS)
+    ok = ovf == 0
+    if sg is not None:
+        assert np.array_equal(sg[ok], esg[ok])
+        assert st["sigma_overflow"] == int(ovf.any())
+    assert st["levels"] == levels
+    assert st["visited"] == int((eS >= 0).sum())
+
+
+def test_arena_mixed_graphs_vs_exact(gpu_available):
+    gs = _mixed_graphs(60, seed=3)
+    rng = np.random.default_rng(4)
+    roots = np.array([int(rng.integers(0, g.n)) for g in gs], dtype=np.int32)
+    with tb.Arena(gs) as a:
+        S, sg, st = a.bfs(roots)
+        for i, (Si, sgi) in enumerate(zip(a.split(S), a.split(sg))):
+            _check_exact(gs[i], roots[i], Si, sgi, st[i])
+        S2, sg2, _ = a.bfs(roots, sigma=False)
+        assert sg2 is None and np.array_equal(S2, S)
+
+
+def test_arena_directed_and_many_launches(gpu_available):
+    """1100 graphs (two launches of up to 1024), directed with duplicate
+    entries and self-loops, so out-lists are built for the pushes."""
+    rng = np.random.default_rng(7)
+    gs = []
+    for i in range(1100):
+        n = int(rng.integers(1, 200))
+        m = int(rng.integers(0, 4 * n + 1))
+        gs.append(graphs.from_edges(n, rng.integers(0, n, m, dtype=np.int32),
+                                    rng.integers(0, n, m, dtype=np.int32)))
+    roots = np.array([int(rng.integers(0, g.n)) for g in gs], dtype=np.int32)
+    with tb.Arena(gs, symmetric=False) as a:
+        S, sg, st = a.bfs(roots)
+        for i, (Si, sgi) in enumerate(zip(a.split(S), a.split(sg))):
+            _check_exact(gs[i], roots[i], Si, sgi, st[i])
+
+
+def test_arena_overflow_flag(gpu_available):
+    gs = [graphs.layered_bipartite(16, 17), graphs.layered_bipartite(16, 16), graphs.rmat(8, 8, seed=1)]
+    with tb.Arena(gs) as a:
+        S, sg, st = a.bfs(np.zeros(3, dtype=np.int32))
+        assert [s["sigma_overflow"] for s in st] == [1, 0, 0]
+        for i, (Si, sgi) in enumerate(zip(a.split(S), a.split(sg))):
+            _check_exact(gs[i], 0, Si, sgi, st[i])
+
+
+def test_arena_invalid_input(gpu_available):
+    bad = graphs.HostCSC(3, np.array([0, 2, 1, 3], np.int32), np.array([1, 2, 0], np.int32), True)
+    with pytest.raises(tb.TbfsError):
+        tb.Arena([graphs.rmat(6, 4, seed=1), bad])
+    with tb.Arena([graphs.rmat(6, 4, seed=1)]) as a:
+        with pytest.raises(tb.TbfsError):
+            a.bfs(np.array([1 << 20], dtype=np.int32))
+
+
+@pytest.fixture(scope="module")
+def served_graphs():
+    rng = np.random.default_rng(11)
+    src = rng.integers(0, 5000, 20000, dtype=np.int32)
+    dst = rng.integers(0, 5000, 20000, dtype=np.int32)
+    hs = [graphs.rmat(14, 16, seed=1), graphs.rmat(12, 16, seed=2), graphs.grid(150, seed=3),
+          graphs.erdos_renyi(20000, 80000, seed=4), graphs.from_edges(5000, src, dst),
+          graphs.layered_bipartite(16, 17)]
+    gs = [tb.Graph.from_host_csc(h) for h in hs]
+    yield hs, gs
+    for g in gs:
+        g.close()
+
+
+def _queries(hs, count, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        gi = int(rng.integers(0, len(hs)))
+        out.append((gi, int(rng.integers(0, hs[gi].n))))
+    return out
+
+
+def test_server_results_equal_alone(gpu_available, served_graphs):
+    hs, gs = served_graphs
+    qs = _queries(hs, 120, seed=1)
+    with tb.Server(max_slots=64, mem_budget=1 << 30) as srv:
+        tickets = [srv.submit(gs[gi], r) for gi, r in qs]
+        results = [srv.wait(t) for t in tickets]
+        c = srv.counters()
+        assert c["completed"] == len(qs) and c["launches"] >= 1
+    for (gi, r), (res, lat) in zip(qs, results):
+        alone = gs[gi].bfs(r)
+        assert np.array_equal(res.S, alone.S), (gi, r)
+        assert np.array_equal(res.sigma, alone.sigma), (gi, r)
+        assert res.stats["levels"] == alone.stats["levels"]
+        assert res.stats["visited"] == alone.stats["visited"]
+        assert res.stats["sigma_overflow"] == alone.stats["sigma_overflow"]
+        assert lat > 0.0
+
+
+def test_server_tight_memory_and_threads(gpu_available, served_graphs):
+    """A budget that holds only a few queries at a time: the rest wait for
+    memory; four host threads submit concurrently; depths-only queries mix
+    with path-count queries."""
+    hs, gs = served_graphs
+    qs = _queries(hs, 80, seed=2)
+    need = max(48 * h.n for h in hs)
+    out = [None] * len(qs)
+    with tb.Server(max_slots=8, mem_budget=3 * need) as srv:
+        def worker(idx):
+            for i in idx:
+                gi, r = qs[i]
+                t = srv.submit(gs[gi], r, sigma=(i % 3 != 0))
+                out[i] = srv.wait(t)
+        ths = [threading.Thread(target=worker, args=(range(k, len(qs), 4),)) for k in range(4)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+    for i, ((gi, r), (res, _)) in enumerate(zip(qs, out)):
+        alone = gs[gi].bfs(r, sigma=(i % 3 != 0))
+        assert np.array_equal(res.S, alone.S)
+        if i % 3 != 0:
+            assert np.array_equal(res.sigma, alone.sigma)
+        else:
+            assert res.sigma is None
+
+
+def test_server_rejects_and_oversized(gpu_available, served_graphs):
+    hs, gs = served_graphs
+    with tb.Server(max_slots=2, mem_budget=256 << 10) as srv:
+        with pytest.raises(tb.TbfsError):
+            srv.submit(gs[0], -1)
+        t = srv.submit(gs[0], 0)  # needs 786 KB, more than the whole pool: fails, does not hang
+        with pytest.raises(tb.TbfsError):
+            srv.wait(t)
+        t2 = srv.submit(gs[4], 0, sigma=False)  # 5000 vertices, depths only: 160 KB, fits
+        res, _ = srv.wait(t2)
+        assert np.array_equal(res.S, gs[4].bfs(0, sigma=False).S)

@@ -5,13 +5,13 @@ computed by one persistent CUDA kernel per traversal, behind the C ABI in
 include/tbfs.h (native) and include/tbfs_compat.h (the reference's entry
 points).  See ``turbobfs_gb300.api`` for the Python face.
 """
-from .api import (COMPAT_FUNCTIONS, BfsResult, Graph, bfs_gpu_bu_csc_sc, bfs_gpu_bu_csc_wa,
+from .api import (COMPAT_FUNCTIONS, Arena, BfsResult, Graph, Server, bfs_gpu_bu_csc_sc, bfs_gpu_bu_csc_wa,
                   bfs_gpu_td_cooc_sc, bfs_gpu_td_csc_sc, bfs_gpu_td_csc_wa, bfs_gpu_tdbu_csc_sc,
                   bfs_gpu_tdbu_csc_wa, device_count, make_options)
 from ._lib import TbfsError, lib
 
 __all__ = [
-    "Graph", "BfsResult", "TbfsError", "lib", "make_options", "device_count",
+    "Graph", "Arena", "Server", "BfsResult", "TbfsError", "lib", "make_options", "device_count",
     "COMPAT_FUNCTIONS", "bfs_gpu_td_csc_sc", "bfs_gpu_td_csc_wa", "bfs_gpu_bu_csc_sc",
     "bfs_gpu_bu_csc_wa", "bfs_gpu_tdbu_csc_sc", "bfs_gpu_tdbu_csc_wa", "bfs_gpu_td_cooc_sc",
 ]

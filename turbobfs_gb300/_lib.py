@@ -91,6 +91,18 @@ _SIGNATURES = {
                               POINTER(Stats)]),
     "tbfs_bfs_batch": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_int32, c_void_p,
                                c_void_p, POINTER(Stats)]),
+    "tbfs_arena_create": (c_int, [c_int32, _P_I32, _P_I64, _P_I32, _P_I32, c_uint32,
+                                  POINTER(c_void_p)]),
+    "tbfs_arena_info": (c_int, [c_void_p, _P_I32, _P_I64, _P_I64]),
+    "tbfs_arena_bfs": (c_int, [c_void_p, _P_I32, POINTER(Options), c_void_p, c_void_p,
+                               POINTER(Stats)]),
+    "tbfs_arena_destroy": (None, [c_void_p]),
+    "tbfs_server_create": (c_int, [c_int32, c_int64, POINTER(Options), POINTER(c_void_p)]),
+    "tbfs_server_submit": (c_int, [c_void_p, c_void_p, c_int32, c_void_p, c_void_p,
+                                   POINTER(c_uint64)]),
+    "tbfs_server_wait": (c_int, [c_void_p, c_uint64, POINTER(Stats), POINTER(c_double)]),
+    "tbfs_server_counters": (c_int, [c_void_p, _P_I64, _P_I64, _P_I64]),
+    "tbfs_server_destroy": (None, [c_void_p]),
     "tbfs_bfs_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64,
                                  c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                  POINTER(Stats)]),

@@ -202,6 +202,122 @@ class Graph:
             pass
 
 
+class Arena:
+    """Many graphs packed in one device arena, one BFS per graph per call
+    (``tbfs_arena_*``).  ``graphs`` is a list of HostCSC (or objects with
+    col_ptr, row_idx, n); S and sigma come back packed in arena order, with
+    ``offsets[i]`` the first vertex of graph i."""
+
+    def __init__(self, graphs, symmetric: bool | None = None):
+        gs = list(graphs)
+        if not gs:
+            raise ValueError("Arena needs at least one graph")
+        if symmetric is None:
+            symmetric = all(getattr(g, "symmetric", False) for g in gs)
+        n = np.array([int(g.n) for g in gs], dtype=np.int32)
+        nnz = np.array([int(np.asarray(g.row_idx).shape[0]) for g in gs], dtype=np.int64)
+        cp = np.concatenate([_i32(g.col_ptr) for g in gs])
+        ic = np.concatenate([_i32(g.row_idx) for g in gs]) if nnz.sum() else np.zeros(1, np.int32)
+        self.n, self.nnz = n, nnz
+        self.offsets = np.concatenate([[0], np.cumsum(n.astype(np.int64))])
+        h = ctypes.c_void_p()
+        check(lib().tbfs_arena_create(len(gs), _ptr(n, _P_I32), _ptr(nnz, _P_I64), _ptr(cp, _P_I32),
+                                      _ptr(ic, _P_I32), GRAPH_SYMMETRIC if symmetric else 0,
+                                      ctypes.byref(h)), "tbfs_arena_create")
+        self._h = h
+
+    def bfs(self, roots, sigma: bool = True, **kw):
+        roots = _i32(roots)
+        if roots.shape[0] != self.n.shape[0]:
+            raise ValueError("one root per graph")
+        o = make_options("td", sigma, **kw)
+        tot = int(self.offsets[-1])
+        S = np.empty(tot, dtype=np.int32)
+        sg = np.empty(tot, dtype=np.int64) if sigma else None
+        stats = (Stats * len(roots))()
+        check(lib().tbfs_arena_bfs(self._h, _ptr(roots, _P_I32), ctypes.byref(o), S.ctypes.data,
+                                   sg.ctypes.data if sg is not None else None, stats),
+              "tbfs_arena_bfs")
+        return S, sg, [stats[i].as_dict() for i in range(len(roots))]
+
+    def split(self, packed):
+        return [packed[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.n))]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().tbfs_arena_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The serving loop (``tbfs_server_*``): submit (graph, root) queries,
+    wait for them; queries admitted while device memory allows run together
+    (continuous batching).  Results land in pinned host buffers."""
+
+    def __init__(self, max_slots: int = 256, mem_budget: int = 8 << 30, **kw):
+        o = make_options("td", True, **kw)
+        h = ctypes.c_void_p()
+        check(lib().tbfs_server_create(int(max_slots), int(mem_budget), ctypes.byref(o),
+                                       ctypes.byref(h)), "tbfs_server_create")
+        self._h = h
+        self._bufs = {}
+
+    def submit(self, graph: "Graph", root: int, sigma: bool = True) -> int:
+        S = np.empty(graph.n, dtype=np.int32)
+        sg = np.empty(graph.n, dtype=np.int64) if sigma else None
+        t = ctypes.c_uint64()
+        check(lib().tbfs_server_submit(self._h, graph.handle, int(root), S.ctypes.data,
+                                       sg.ctypes.data if sg is not None else None,
+                                       ctypes.byref(t)), "tbfs_server_submit")
+        self._bufs[t.value] = (S, sg)
+        return t.value
+
+    def wait(self, ticket: int):
+        """(BfsResult, latency_ms) of a submitted query."""
+        st = Stats()
+        lat = ctypes.c_double()
+        rc = lib().tbfs_server_wait(self._h, ctypes.c_uint64(ticket), ctypes.byref(st),
+                                    ctypes.byref(lat))
+        S, sg = self._bufs.pop(ticket)
+        check(rc, "tbfs_server_wait")
+        return BfsResult(S, sg, st.as_dict()), lat.value
+
+    def counters(self) -> dict:
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        check(lib().tbfs_server_counters(self._h, ctypes.byref(a), ctypes.byref(b),
+                                         ctypes.byref(c)), "tbfs_server_counters")
+        return {"launches": a.value, "levels": b.value, "completed": c.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            lib().tbfs_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------- compat ---
 # Same names, argument order and in-place outputs as the reference's C
 # functions; the int return is 0 on success, a tbfs_status code otherwise.

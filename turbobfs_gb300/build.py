@@ -21,7 +21,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "libtbfs.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["bfs_engine.cu", "batch_engine.cu", "graph_ingest.cu", "api.cu", "batch_api.cu", "noalloc.cu"]
+CU_SOURCES = ["bfs_engine.cu", "batch_engine.cu", "multi_engine.cu", "graph_ingest.cu", "api.cu",
+              "batch_api.cu", "multi_api.cu", "noalloc.cu"]
 C_SOURCES = ["host_graph.c"]
 
 

@@ -1,0 +1,768 @@
+/*
+ * multi_api.cu -- the C ABI over the multi-instance engine (multi_engine.cu):
+ *
+ *   tbfs_arena_*   many graphs packed in one int32 offset arena, one root
+ *                  each, all traversed in one persistent launch;
+ *   tbfs_server_*  a request loop on its own host thread: (graph, root)
+ *                  queries are admitted into free instance slots while the
+ *                  server's device-memory pool has room, advance level by
+ *                  level together with the queries already running
+ *                  (continuous batching at level granularity), and retire as
+ *                  they finish, with their latency recorded.
+ *
+ * Neither has a counterpart in the reference, which traverses one root of
+ * one graph per call (TurboBFS_CSC_TD/bfsgputdcsc_sc.cu:47-149).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "tbfs.h"
+#include "tbfs_internal.h"
+
+using tbfs::InstDesc;
+using tbfs::LaunchGeom;
+using tbfs::MultiCtl;
+using tbfs::MultiParams;
+
+namespace {
+
+tbfs_status mfail(cudaError_t e, const char *what) {
+  tbfs_set_error("%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? TBFS_ERR_OUT_OF_MEMORY : TBFS_ERR_CUDA;
+}
+
+#define MTRY(call, what)                             \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return mfail(e_, what);   \
+  } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+/* Per-traversal device buffers inside one block: S, sig, q[3], e[3]. */
+size_t inst_bytes(int n, bool sigma) {
+  const size_t nn = (size_t)n;
+  return align256(nn * 4) + (sigma ? align256(nn * 8) : 0) + 6 * align256(nn * 4);
+}
+
+void carve(unsigned char *base, int n, bool sigma, InstDesc &D) {
+  const size_t nn = (size_t)n;
+  size_t off = 0;
+  D.S = reinterpret_cast<int *>(base + off);
+  off += align256(nn * 4);
+  D.sig = nullptr;
+  if (sigma) {
+    D.sig = reinterpret_cast<unsigned long long *>(base + off);
+    off += align256(nn * 8);
+  }
+  for (int b = 0; b < 3; ++b) {
+    D.q[b] = reinterpret_cast<int *>(base + off);
+    off += align256(nn * 4);
+    D.e[b] = reinterpret_cast<unsigned *>(base + off);
+    off += align256(nn * 4);
+  }
+}
+
+void fill_stats(const InstDesc &D, float ms, tbfs_stats *st) {
+  memset(st, 0, sizeof(*st));
+  st->levels = D.levels;
+  st->td_levels = D.levels;
+  st->bu_levels = 0;
+  st->sigma_overflow = D.ovf;
+  st->visited = D.visited;
+  st->edges = D.edges;
+  st->device_ms = ms;
+}
+
+/* host-side transpose of one CSC (in-lists) into out-lists */
+void transpose_csc(int n, const int32_t *cp, const int32_t *ic, std::vector<int32_t> &rp,
+                   std::vector<int32_t> &jr) {
+  const int64_t nnz = cp[n];
+  rp.assign((size_t)n + 1, 0);
+  jr.assign((size_t)nnz, 0);
+  for (int64_t k = 0; k < nnz; ++k) rp[(size_t)ic[k] + 1]++;
+  for (int v = 0; v < n; ++v) rp[(size_t)v + 1] += rp[(size_t)v];
+  std::vector<int32_t> fill(rp.begin(), rp.end() - 1);
+  for (int v = 0; v < n; ++v)
+    for (int64_t k = cp[v]; k < cp[v + 1]; ++k) jr[(size_t)fill[(size_t)ic[k]]++] = v;
+}
+
+}  // namespace
+
+/* =============================================================== arena */
+
+struct tbfs_arena {
+  int device = 0;
+  int32_t g = 0;
+  bool symmetric = false;
+  std::vector<int32_t> n;
+  std::vector<int64_t> nnz, voff, eoff; /* vertex / entry offsets of graph i */
+  int64_t nv = 0, ne = 0;
+  int *cp = nullptr, *ic = nullptr, *rp = nullptr, *jr = nullptr; /* packed */
+  unsigned char *work = nullptr; /* per-graph traversal blocks */
+  std::vector<size_t> woff;
+  bool work_sigma = false;
+  InstDesc *inst = nullptr, *inst_host = nullptr;
+  int *slots = nullptr;
+  MultiCtl *ctl = nullptr, *ctl_host = nullptr;
+  LaunchGeom geom;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+static void arena_free(tbfs_arena *a) {
+  if (!a) return;
+  cudaSetDevice(a->device);
+  cudaFree(a->cp);
+  cudaFree(a->ic);
+  if (!a->symmetric) {
+    cudaFree(a->rp);
+    cudaFree(a->jr);
+  }
+  cudaFree(a->work);
+  cudaFree(a->inst);
+  cudaFree(a->slots);
+  cudaFree(a->ctl);
+  if (a->inst_host) cudaFreeHost(a->inst_host);
+  if (a->ctl_host) cudaFreeHost(a->ctl_host);
+  if (a->ev0) cudaEventDestroy(a->ev0);
+  if (a->ev1) cudaEventDestroy(a->ev1);
+  delete a;
+}
+
+extern "C" void tbfs_arena_destroy(tbfs_arena *a) { arena_free(a); }
+
+static tbfs_status arena_build(tbfs_arena *a, const int32_t *col_ptr, const int32_t *row_idx) {
+  MTRY(cudaGetDevice(&a->device), "cudaGetDevice");
+  /* validate every graph on the host and pack its out-lists if needed */
+  std::vector<int32_t> rp_all, jr_all;
+  if (!a->symmetric) {
+    rp_all.reserve((size_t)(a->nv + a->g));
+    jr_all.reserve((size_t)a->ne);
+  }
+  for (int32_t i = 0; i < a->g; ++i) {
+    const int32_t *cp = col_ptr + a->voff[i] + i;
+    const int32_t *ic = row_idx + a->eoff[i];
+    const int32_t n = a->n[i];
+    if (cp[0] != 0 || cp[n] != a->nnz[i]) {
+      tbfs_set_error("tbfs_arena_create: graph %d: col_ptr must start at 0 and end at nnz", i);
+      return TBFS_ERR_INVALID_ARG;
+    }
+    for (int32_t v = 0; v < n; ++v)
+      if (cp[v + 1] < cp[v]) {
+        tbfs_set_error("tbfs_arena_create: graph %d: col_ptr decreases at %d", i, v);
+        return TBFS_ERR_INVALID_ARG;
+      }
+    for (int64_t k = 0; k < a->nnz[i]; ++k)
+      if (ic[k] < 0 || ic[k] >= n) {
+        tbfs_set_error("tbfs_arena_create: graph %d: row index out of range", i);
+        return TBFS_ERR_INVALID_ARG;
+      }
+    if (!a->symmetric) {
+      std::vector<int32_t> rp, jr;
+      transpose_csc(n, cp, ic, rp, jr);
+      rp_all.insert(rp_all.end(), rp.begin(), rp.end());
+      jr_all.insert(jr_all.end(), jr.begin(), jr.end());
+    }
+  }
+  const size_t ncp = (size_t)(a->nv + a->g);
+  MTRY(cudaMalloc(&a->cp, ncp * sizeof(int)), "arena alloc");
+  MTRY(cudaMalloc(&a->ic, std::max<size_t>((size_t)a->ne, 1) * sizeof(int)), "arena alloc");
+  MTRY(cudaMemcpy(a->cp, col_ptr, ncp * sizeof(int), cudaMemcpyHostToDevice), "arena upload");
+  if (a->ne)
+    MTRY(cudaMemcpy(a->ic, row_idx, (size_t)a->ne * sizeof(int), cudaMemcpyHostToDevice),
+         "arena upload");
+  if (a->symmetric) {
+    a->rp = a->cp;
+    a->jr = a->ic;
+  } else {
+    MTRY(cudaMalloc(&a->rp, ncp * sizeof(int)), "arena alloc");
+    MTRY(cudaMalloc(&a->jr, std::max<size_t>((size_t)a->ne, 1) * sizeof(int)), "arena alloc");
+    MTRY(cudaMemcpy(a->rp, rp_all.data(), ncp * sizeof(int), cudaMemcpyHostToDevice),
+         "arena upload");
+    if (a->ne)
+      MTRY(cudaMemcpy(a->jr, jr_all.data(), (size_t)a->ne * sizeof(int), cudaMemcpyHostToDevice),
+           "arena upload");
+  }
+  const int slots = std::min<int32_t>(a->g, tbfs::kMultiMaxSlots);
+  MTRY(cudaMalloc(&a->inst, (size_t)slots * sizeof(InstDesc)), "arena alloc");
+  MTRY(cudaMallocHost(&a->inst_host, (size_t)slots * sizeof(InstDesc)), "arena alloc");
+  MTRY(cudaMalloc(&a->slots, (size_t)slots * sizeof(int)), "arena alloc");
+  MTRY(cudaMalloc(&a->ctl, sizeof(MultiCtl)), "arena alloc");
+  MTRY(cudaMallocHost(&a->ctl_host, sizeof(MultiCtl)), "arena alloc");
+  MTRY(cudaEventCreate(&a->ev0), "event");
+  MTRY(cudaEventCreate(&a->ev1), "event");
+  MTRY(tbfs::multi_geometry(a->device, &a->geom), "launch geometry");
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_arena_create(int32_t g, const int32_t *n, const int64_t *nnz,
+                                         const int32_t *col_ptr, const int32_t *row_idx,
+                                         uint32_t flags, tbfs_arena **out) {
+  if (!out) return TBFS_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (g < 1 || !n || !nnz || !col_ptr || !row_idx) {
+    tbfs_set_error("tbfs_arena_create: need g >= 1 and all arrays");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  int dc = 0;
+  if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) {
+    cudaGetLastError();
+    tbfs_set_error("no CUDA device visible");
+    return TBFS_ERR_NO_DEVICE;
+  }
+  tbfs_arena *a = new tbfs_arena();
+  a->g = g;
+  a->symmetric = (flags & TBFS_GRAPH_SYMMETRIC) != 0;
+  a->n.assign(n, n + g);
+  a->nnz.assign(nnz, nnz + g);
+  a->voff.resize((size_t)g);
+  a->eoff.resize((size_t)g);
+  for (int32_t i = 0; i < g; ++i) {
+    if (n[i] < 1 || nnz[i] < 0 || nnz[i] > INT32_MAX) {
+      arena_free(a);
+      tbfs_set_error("tbfs_arena_create: graph %d: need n >= 1 and 0 <= nnz <= INT32_MAX", i);
+      return TBFS_ERR_INVALID_ARG;
+    }
+    a->voff[(size_t)i] = a->nv;
+    a->eoff[(size_t)i] = a->ne;
+    a->nv += n[i];
+    a->ne += nnz[i];
+  }
+  if (a->nv + g > INT32_MAX || a->ne > INT32_MAX) {
+    arena_free(a);
+    tbfs_set_error("tbfs_arena_create: the packed arena exceeds int32 offsets");
+    return TBFS_ERR_UNSUPPORTED;
+  }
+  tbfs_status st = arena_build(a, col_ptr, row_idx);
+  if (st != TBFS_OK) {
+    arena_free(a);
+    return st;
+  }
+  *out = a;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_arena_info(const tbfs_arena *a, int32_t *g, int64_t *vertices,
+                                       int64_t *entries) {
+  if (!a) return TBFS_ERR_INVALID_ARG;
+  if (g) *g = a->g;
+  if (vertices) *vertices = a->nv;
+  if (entries) *entries = a->ne;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_arena_bfs(tbfs_arena *a, const int32_t *roots, const tbfs_options *opt,
+                                      int32_t *S, int64_t *sigma, tbfs_stats *stats) {
+  tbfs_options o;
+  tbfs_options_init(&o);
+  if (opt) o = *opt;
+  if (!a || !roots || !S || (o.want_sigma && !sigma)) {
+    tbfs_set_error("tbfs_arena_bfs: null arena, roots or outputs");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  for (int32_t i = 0; i < a->g; ++i)
+    if (roots[i] < 0 || roots[i] >= a->n[(size_t)i]) {
+      tbfs_set_error("tbfs_arena_bfs: root of graph %d outside [0, n)", i);
+      return TBFS_ERR_INVALID_ARG;
+    }
+  MTRY(cudaSetDevice(a->device), "cudaSetDevice");
+  const bool want_sigma = o.want_sigma != 0;
+  cudaStream_t s = (cudaStream_t)o.stream;
+  if (!a->work || (want_sigma && !a->work_sigma)) {
+    cudaFree(a->work);
+    a->work = nullptr;
+    a->woff.assign((size_t)a->g, 0);
+    size_t tot = 0;
+    for (int32_t i = 0; i < a->g; ++i) {
+      a->woff[(size_t)i] = tot;
+      tot += inst_bytes(a->n[(size_t)i], want_sigma);
+    }
+    MTRY(cudaMalloc(&a->work, tot), "arena traversal buffers");
+    a->work_sigma = want_sigma;
+  }
+  const long long timeout = o.timeout_ns > 0 ? o.timeout_ns : 4000000000LL;
+  const int cap = tbfs::kMultiMaxSlots;
+  for (int32_t g0 = 0; g0 < a->g; g0 += cap) {
+    const int k = std::min<int32_t>(cap, a->g - g0);
+    std::vector<int> ids((size_t)k);
+    for (int j = 0; j < k; ++j) {
+      const int i = g0 + j;
+      InstDesc &D = a->inst_host[j];
+      memset(&D, 0, sizeof(D));
+      D.cp = a->cp + a->voff[(size_t)i] + i;
+      D.ic = a->ic + a->eoff[(size_t)i];
+      D.rp = a->rp + a->voff[(size_t)i] + i;
+      D.jr = a->jr + a->eoff[(size_t)i];
+      D.inv = nullptr;
+      D.nnz = a->nnz[(size_t)i];
+      D.n = a->n[(size_t)i];
+      D.root = roots[i];
+      carve(a->work + a->woff[(size_t)i], D.n, want_sigma, D);
+      MTRY(cudaMemsetAsync(D.S, 0xff, (size_t)D.n * sizeof(int), s), "clear S");
+      if (D.sig) MTRY(cudaMemsetAsync(D.sig, 0, (size_t)D.n * 8, s), "clear sigma");
+      ids[(size_t)j] = j;
+    }
+    MTRY(cudaMemcpyAsync(a->inst, a->inst_host, (size_t)k * sizeof(InstDesc),
+                         cudaMemcpyHostToDevice, s),
+         "descriptors");
+    MTRY(cudaMemcpyAsync(a->slots, ids.data(), (size_t)k * sizeof(int), cudaMemcpyHostToDevice, s),
+         "slots");
+    MTRY(tbfs::multi_init(a->inst, a->slots, k, s), "init");
+    MTRY(cudaMemsetAsync(a->ctl, 0, sizeof(MultiCtl), s), "clear control block");
+    MultiParams p;
+    p.inst = a->inst;
+    p.nslots = k;
+    p.max_phases = INT32_MAX;
+    p.ctl = a->ctl;
+    p.timeout_ns = timeout;
+    MTRY(cudaEventRecord(a->ev0, s), "event");
+    MTRY(tbfs::multi_launch(p, a->geom, s), "multi launch");
+    MTRY(cudaEventRecord(a->ev1, s), "event");
+    MTRY(cudaMemcpyAsync(a->inst_host, a->inst, (size_t)k * sizeof(InstDesc),
+                         cudaMemcpyDeviceToHost, s),
+         "read descriptors");
+    MTRY(cudaMemcpyAsync(a->ctl_host, a->ctl, sizeof(MultiCtl), cudaMemcpyDeviceToHost, s),
+         "read control block");
+    /* results: the packed layout is the arena's own (no renumbering) */
+    for (int j = 0; j < k; ++j) {
+      const int i = g0 + j;
+      const InstDesc &D = a->inst_host[j];
+      const size_t vo = (size_t)a->voff[(size_t)i];
+      const cudaMemcpyKind kind = o.outputs_on_device ? cudaMemcpyDeviceToDevice
+                                                      : cudaMemcpyDeviceToHost;
+      MTRY(cudaMemcpyAsync(S + vo, D.S, (size_t)D.n * sizeof(int), kind, s), "copy S");
+      if (want_sigma)
+        MTRY(cudaMemcpyAsync(sigma + vo, D.sig, (size_t)D.n * 8, kind, s), "copy sigma");
+    }
+    MTRY(cudaStreamSynchronize(s), "arena traversal");
+    if (a->ctl_host->status != 0) {
+      tbfs_set_error("tbfs_arena_bfs: grid barrier wait exceeded its budget");
+      return TBFS_ERR_TIMEOUT;
+    }
+    float ms = 0.0f;
+    MTRY(cudaEventElapsedTime(&ms, a->ev0, a->ev1), "event time");
+    if (stats)
+      for (int j = 0; j < k; ++j) fill_stats(a->inst_host[j], ms, &stats[g0 + j]);
+  }
+  return TBFS_OK;
+}
+
+/* ============================================================== server */
+
+namespace {
+
+struct Request {
+  uint64_t ticket = 0;
+  tbfs_graph *g = nullptr;
+  int32_t root = 0;
+  int32_t *S = nullptr;
+  int64_t *sigma = nullptr;
+  std::chrono::steady_clock::time_point t_submit;
+  /* filled on completion */
+  bool done = false;
+  tbfs_status status = TBFS_OK;
+  tbfs_stats stats = {};
+  double latency_ms = 0.0;
+};
+
+/* first-fit allocator over [0, size) */
+class Pool {
+ public:
+  void reset(size_t size) {
+    free_.clear();
+    if (size) free_[0] = size;
+  }
+  bool alloc(size_t bytes, size_t *off) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        *off = it->first;
+        const size_t rest = it->second - bytes, at = it->first + bytes;
+        free_.erase(it);
+        if (rest) free_[at] = rest;
+        return true;
+      }
+    }
+    return false;
+  }
+  void release(size_t off, size_t bytes) {
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+
+ private:
+  std::map<size_t, size_t> free_;
+};
+
+struct Slot {
+  bool busy = false;
+  std::shared_ptr<Request> req;
+  size_t off = 0, bytes = 0;
+};
+
+}  // namespace
+
+struct tbfs_server {
+  int device = 0;
+  int max_slots = 0;
+  size_t budget = 0;
+  tbfs_options opt;
+  unsigned char *mem = nullptr;
+  Pool pool;
+  std::vector<Slot> slots;
+  InstDesc *inst = nullptr, *inst_host = nullptr;
+  int *slot_ids = nullptr, *slot_ids_host = nullptr;
+  MultiCtl *ctl = nullptr, *ctl_host = nullptr;
+  LaunchGeom geom;
+  cudaStream_t stream = nullptr;
+  /* request queue */
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::shared_ptr<Request>> pending;
+  std::unordered_map<uint64_t, std::shared_ptr<Request>> by_ticket;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  tbfs_status fatal = TBFS_OK;
+  std::thread worker;
+  /* counters */
+  long long launches = 0, levels_run = 0, completed = 0;
+  double device_ms = 0.0;
+};
+
+namespace {
+
+/* one step of the loop: admit, advance every instance up to max_phases
+ * levels in one launch, retire the finished ones */
+tbfs_status server_step(tbfs_server *sv, bool *idle) {
+  std::vector<int> admitted;
+  int waiting = 0;
+  {
+    std::unique_lock<std::mutex> lk(sv->mu);
+    while (!sv->pending.empty()) {
+      auto &r = sv->pending.front();
+      const bool sigma = r->sigma != nullptr;
+      const size_t need = inst_bytes(r->g->n, sigma) + align256((size_t)r->g->n * 4) +
+                          (sigma ? align256((size_t)r->g->n * 8) : 0); /* + caller-order copy */
+      int free_slot = -1;
+      for (int i = 0; i < sv->max_slots; ++i)
+        if (!sv->slots[(size_t)i].busy) {
+          free_slot = i;
+          break;
+        }
+      if (free_slot < 0) break;
+      size_t off = 0;
+      if (need > sv->budget) { /* can never fit: fail it */
+        r->status = TBFS_ERR_OUT_OF_MEMORY;
+        r->done = true;
+        sv->pending.pop_front();
+        sv->cv_done.notify_all();
+        continue;
+      }
+      if (!sv->pool.alloc(need, &off)) break; /* wait for memory to free up */
+      Slot &sl = sv->slots[(size_t)free_slot];
+      sl.busy = true;
+      sl.req = r;
+      sl.off = off;
+      sl.bytes = need;
+      admitted.push_back(free_slot);
+      sv->pending.pop_front();
+    }
+    waiting = (int)sv->pending.size();
+  }
+  cudaStream_t s = sv->stream;
+  for (int i : admitted) {
+    Slot &sl = sv->slots[(size_t)i];
+    const Request &r = *sl.req;
+    InstDesc &D = sv->inst_host[i];
+    memset(&D, 0, sizeof(D));
+    D.cp = r.g->cp;
+    D.ic = r.g->ic;
+    D.rp = r.g->rp;
+    D.jr = r.g->jr;
+    D.inv = r.g->inv;
+    D.nnz = r.g->nnz;
+    D.n = r.g->n;
+    D.root = r.root;
+    carve(sv->mem + sl.off, D.n, r.sigma != nullptr, D);
+    MTRY(cudaMemsetAsync(D.S, 0xff, (size_t)D.n * sizeof(int), s), "clear S");
+    if (D.sig) MTRY(cudaMemsetAsync(D.sig, 0, (size_t)D.n * 8, s), "clear sigma");
+  }
+  int nslots = 0;
+  for (int i = 0; i < sv->max_slots; ++i) {
+    if (sv->slots[(size_t)i].busy)
+      nslots = i + 1;
+    else
+      sv->inst_host[i].done = 1; /* empty */
+  }
+  *idle = nslots == 0;
+  if (nslots == 0) return TBFS_OK;
+  MTRY(cudaMemcpyAsync(sv->inst, sv->inst_host, (size_t)nslots * sizeof(InstDesc),
+                       cudaMemcpyHostToDevice, s),
+       "descriptors");
+  if (!admitted.empty()) {
+    for (size_t j = 0; j < admitted.size(); ++j) sv->slot_ids_host[j] = admitted[j];
+    MTRY(cudaMemcpyAsync(sv->slot_ids, sv->slot_ids_host, admitted.size() * sizeof(int),
+                         cudaMemcpyHostToDevice, s),
+         "slots");
+    MTRY(tbfs::multi_init(sv->inst, sv->slot_ids, (int)admitted.size(), s), "init");
+  }
+  /* quantum: few levels while requests wait for a slot or memory, so that
+   * they are admitted soon; otherwise run long */
+  MultiParams p;
+  p.inst = sv->inst;
+  p.nslots = nslots;
+  p.max_phases = waiting > 0 ? 4 : 1 << 16;
+  p.ctl = sv->ctl;
+  p.timeout_ns = sv->opt.timeout_ns > 0 ? sv->opt.timeout_ns : 4000000000LL;
+  MTRY(cudaMemsetAsync(sv->ctl, 0, sizeof(MultiCtl), s), "clear control block");
+  MTRY(tbfs::multi_launch(p, sv->geom, s), "multi launch");
+  MTRY(cudaMemcpyAsync(sv->inst_host, sv->inst, (size_t)nslots * sizeof(InstDesc),
+                       cudaMemcpyDeviceToHost, s),
+       "read descriptors");
+  MTRY(cudaMemcpyAsync(sv->ctl_host, sv->ctl, sizeof(MultiCtl), cudaMemcpyDeviceToHost, s),
+       "read control block");
+  MTRY(cudaStreamSynchronize(s), "server step");
+  sv->launches++;
+  sv->levels_run += sv->ctl_host->phases;
+  if (sv->ctl_host->status != 0) {
+    tbfs_set_error("tbfs_server: grid barrier wait exceeded its budget");
+    return TBFS_ERR_TIMEOUT;
+  }
+  /* retire: results in the caller's numbering, into the caller's buffers */
+  std::vector<int> finished;
+  for (int i = 0; i < nslots; ++i) {
+    Slot &sl = sv->slots[(size_t)i];
+    if (!sl.busy || !sv->inst_host[i].done) continue;
+    const InstDesc &D = sv->inst_host[i];
+    Request &r = *sl.req;
+    /* the caller-order copy sits after the traversal buffers of the block */
+    unsigned char *tail = sv->mem + sl.off + inst_bytes(D.n, D.sig != nullptr);
+    int *S_c = reinterpret_cast<int *>(tail);
+    unsigned long long *sig_c =
+        D.sig ? reinterpret_cast<unsigned long long *>(tail + align256((size_t)D.n * 4)) : nullptr;
+    MTRY(tbfs::multi_gather(D.S, D.sig, D.inv, D.n, S_c, sig_c, s), "gather");
+    MTRY(cudaMemcpyAsync(r.S, S_c, (size_t)D.n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy S");
+    if (sig_c)
+      MTRY(cudaMemcpyAsync(r.sigma, sig_c, (size_t)D.n * 8, cudaMemcpyDeviceToHost, s),
+           "copy sigma");
+    finished.push_back(i);
+  }
+  if (finished.empty()) return TBFS_OK;
+  MTRY(cudaStreamSynchronize(s), "copy results");
+  const auto now = std::chrono::steady_clock::now();
+  std::lock_guard<std::mutex> lk(sv->mu);
+  for (int i : finished) {
+    Slot &sl = sv->slots[(size_t)i];
+    Request &r = *sl.req;
+    fill_stats(sv->inst_host[i], 0.0f, &r.stats);
+    r.latency_ms = std::chrono::duration<double, std::milli>(now - r.t_submit).count();
+    r.status = TBFS_OK;
+    r.done = true;
+    sv->pool.release(sl.off, sl.bytes);
+    sl.busy = false;
+    sl.req.reset();
+    sv->completed++;
+  }
+  sv->cv_done.notify_all();
+  return TBFS_OK;
+}
+
+void server_loop(tbfs_server *sv) {
+  cudaSetDevice(sv->device);
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      bool any_busy = false;
+      for (const Slot &sl : sv->slots) any_busy |= sl.busy;
+      sv->cv_work.wait(lk, [&] { return sv->stop || !sv->pending.empty() || any_busy; });
+      if (sv->stop && sv->pending.empty() && !any_busy) return;
+      if (sv->stop) {
+        /* fail what is still queued, finish nothing new */
+        for (auto &r : sv->pending) {
+          r->status = TBFS_ERR_INVALID_ARG;
+          r->done = true;
+        }
+        sv->pending.clear();
+        sv->cv_done.notify_all();
+        if (!any_busy) return;
+      }
+    }
+    bool idle = false;
+    const tbfs_status st = server_step(sv, &idle);
+    if (st != TBFS_OK) {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->fatal = st;
+      for (Slot &sl : sv->slots)
+        if (sl.busy) {
+          sl.req->status = st;
+          sl.req->done = true;
+          sl.busy = false;
+          sl.req.reset();
+        }
+      for (auto &r : sv->pending) {
+        r->status = st;
+        r->done = true;
+      }
+      sv->pending.clear();
+      sv->cv_done.notify_all();
+      return;
+    }
+  }
+}
+
+void server_free(tbfs_server *sv) {
+  if (!sv) return;
+  cudaSetDevice(sv->device);
+  cudaFree(sv->mem);
+  cudaFree(sv->inst);
+  cudaFree(sv->slot_ids);
+  cudaFree(sv->ctl);
+  if (sv->inst_host) cudaFreeHost(sv->inst_host);
+  if (sv->slot_ids_host) cudaFreeHost(sv->slot_ids_host);
+  if (sv->ctl_host) cudaFreeHost(sv->ctl_host);
+  if (sv->stream) cudaStreamDestroy(sv->stream);
+  delete sv;
+}
+
+tbfs_status server_init(tbfs_server *sv) {
+  MTRY(cudaGetDevice(&sv->device), "cudaGetDevice");
+  MTRY(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking), "stream");
+  MTRY(cudaMalloc(&sv->mem, sv->budget), "server memory pool");
+  sv->pool.reset(sv->budget);
+  MTRY(cudaMalloc(&sv->inst, (size_t)sv->max_slots * sizeof(InstDesc)), "alloc");
+  MTRY(cudaMallocHost(&sv->inst_host, (size_t)sv->max_slots * sizeof(InstDesc)), "alloc");
+  memset(sv->inst_host, 0, (size_t)sv->max_slots * sizeof(InstDesc));
+  MTRY(cudaMalloc(&sv->slot_ids, (size_t)sv->max_slots * sizeof(int)), "alloc");
+  MTRY(cudaMallocHost(&sv->slot_ids_host, (size_t)sv->max_slots * sizeof(int)), "alloc");
+  MTRY(cudaMalloc(&sv->ctl, sizeof(MultiCtl)), "alloc");
+  MTRY(cudaMallocHost(&sv->ctl_host, sizeof(MultiCtl)), "alloc");
+  MTRY(tbfs::multi_geometry(sv->device, &sv->geom), "launch geometry");
+  sv->slots.assign((size_t)sv->max_slots, Slot());
+  return TBFS_OK;
+}
+
+}  // namespace
+
+extern "C" tbfs_status tbfs_server_create(int32_t max_slots, int64_t mem_budget,
+                                          const tbfs_options *opt, tbfs_server **out) {
+  if (!out) return TBFS_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (max_slots < 1 || max_slots > tbfs::kMultiMaxSlots || mem_budget < 1) {
+    tbfs_set_error("tbfs_server_create: need 1 <= max_slots <= %d and mem_budget > 0",
+                   tbfs::kMultiMaxSlots);
+    return TBFS_ERR_INVALID_ARG;
+  }
+  int dc = 0;
+  if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) {
+    cudaGetLastError();
+    tbfs_set_error("no CUDA device visible");
+    return TBFS_ERR_NO_DEVICE;
+  }
+  tbfs_server *sv = new tbfs_server();
+  sv->max_slots = max_slots;
+  sv->budget = (size_t)mem_budget;
+  tbfs_options_init(&sv->opt);
+  if (opt) sv->opt = *opt;
+  tbfs_status st = server_init(sv);
+  if (st != TBFS_OK) {
+    server_free(sv);
+    return st;
+  }
+  sv->worker = std::thread(server_loop, sv);
+  *out = sv;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_server_submit(tbfs_server *sv, tbfs_graph *g, int32_t root,
+                                          int32_t *S, int64_t *sigma, uint64_t *ticket) {
+  if (!sv || !g || !S || !ticket) {
+    tbfs_set_error("tbfs_server_submit: null server, graph, S or ticket");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  if (root < 0 || root >= g->n) {
+    tbfs_set_error("tbfs_server_submit: root outside [0, n)");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  if (g->device != sv->device) {
+    tbfs_set_error("tbfs_server_submit: graph lives on another device");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  auto r = std::make_shared<Request>();
+  r->g = g;
+  r->root = root;
+  r->S = S;
+  r->sigma = sigma;
+  r->t_submit = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->stop || sv->fatal != TBFS_OK) {
+      tbfs_set_error("tbfs_server_submit: server stopped");
+      return sv->fatal != TBFS_OK ? sv->fatal : TBFS_ERR_INVALID_ARG;
+    }
+    r->ticket = sv->next_ticket++;
+    sv->by_ticket[r->ticket] = r;
+    sv->pending.push_back(r);
+  }
+  sv->cv_work.notify_one();
+  *ticket = r->ticket;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_server_wait(tbfs_server *sv, uint64_t ticket, tbfs_stats *stats,
+                                        double *latency_ms) {
+  if (!sv) return TBFS_ERR_INVALID_ARG;
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto it = sv->by_ticket.find(ticket);
+  if (it == sv->by_ticket.end()) {
+    tbfs_set_error("tbfs_server_wait: unknown ticket");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  std::shared_ptr<Request> r = it->second;
+  sv->cv_done.wait(lk, [&] { return r->done; });
+  sv->by_ticket.erase(it);
+  if (stats) *stats = r->stats;
+  if (latency_ms) *latency_ms = r->latency_ms;
+  return r->status;
+}
+
+extern "C" tbfs_status tbfs_server_counters(tbfs_server *sv, int64_t *launches, int64_t *levels,
+                                            int64_t *completed) {
+  if (!sv) return TBFS_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (launches) *launches = sv->launches;
+  if (levels) *levels = sv->levels_run;
+  if (completed) *completed = sv->completed;
+  return TBFS_OK;
+}
+
+extern "C" void tbfs_server_destroy(tbfs_server *sv) {
+  if (!sv) return;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+  }
+  sv->cv_work.notify_all();
+  if (sv->worker.joinable()) sv->worker.join();
+  server_free(sv);
+}

@@ -1,0 +1,303 @@
+/*
+ * multi_engine.cu -- many independent traversals, each (graph, root) its own
+ * instance, advancing together in one persistent cooperative launch: one
+ * grid barrier per level for all of them.  Instances may live on different
+ * graphs (a packed arena of many small graphs, or separately resident
+ * graphs of a server) and start at different times: every instance keeps its
+ * own level counter, queues and statistics in its descriptor, so a launch can
+ * stop after a number of levels and a later launch can carry on with new
+ * instances admitted beside the unfinished ones (continuous batching).
+ *
+ * Per level and instance the step is the reference's top-down semiring
+ * iteration (TurboBFS_CSC_TD/bfsgputdcsc_sc.cu:159-208: f_t = A^T f over the
+ * frontier, sigma += f, S = d), done as a push over the out-edges of the
+ * instance's frontier queue:
+ *   - an edge u -> v with S[v] == -1 claims v with atomicCAS(S[v], -1, d+1)
+ *     and appends it to the next queue;
+ *   - every edge that lands on a vertex at depth d+1 (claimed now, by this
+ *     edge or another) adds sigma[u] to sigma[v] with a 64-bit atomicAdd;
+ *     sigma[u] is final because u was claimed a level earlier.
+ * Work is edge-balanced across all instances: each CTA computes the same
+ * prefix of per-instance work items (kItemEdges consecutive frontier
+ * out-edges) in shared memory; a warp claims item indices from a global
+ * counter and locates its instance by binary search in that prefix, the
+ * owner of each edge by a 32-ary search over the instance's out-degree
+ * prefix followed by a shuffle search in a 32-entry window.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "tbfs_internal.h"
+
+namespace tbfs {
+namespace {
+
+using dev::FULL;
+using dev::grid_barrier;
+
+constexpr int kBlock = 256;
+constexpr int kRounds = 8;                /* 32-edge rounds per item */
+constexpr unsigned kItemEdges = 32 * kRounds;
+
+/* Append, for every lane with take set, (v, out-degree dg) to a queue:
+ * one 64-bit atomic per warp reserves (count << 32 | edge sum).  All 32
+ * lanes call. */
+__device__ __forceinline__ void enqueue(bool take, int v, unsigned dg, int *q, unsigned *e,
+                                        unsigned long long *ctr) {
+  const int lane = threadIdx.x & 31;
+  const unsigned bal = __ballot_sync(FULL, take);
+  if (!bal) return;
+  const unsigned mine = take ? dg : 0u;
+  unsigned inc = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned t = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += t;
+  }
+  const unsigned tot = __shfl_sync(FULL, inc, 31);
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(ctr, ((unsigned long long)__popc(bal) << 32) | tot);
+  base = __shfl_sync(FULL, base, 0);
+  if (take) {
+    const unsigned pos = (unsigned)(base >> 32) + __popc(bal & ((1u << lane) - 1u));
+    q[pos] = v;
+    e[pos] = (unsigned)base + inc - mine;
+  }
+}
+
+/* largest o < cnt with e[o] <= t, per lane (fallback of the window search) */
+__device__ __forceinline__ unsigned lane_owner(const unsigned *e, unsigned cnt, unsigned t) {
+  unsigned lo = 0, hi = cnt;
+  while (hi - lo > 1) {
+    const unsigned mid = (lo + hi) >> 1;
+    if (__ldcg(e + mid) <= t)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) {
+  __shared__ unsigned s_pre[kMultiMaxSlots + 1]; /* item prefix over slots      */
+  __shared__ int s_d[kMultiMaxSlots];            /* level each slot runs next   */
+  __shared__ unsigned s_qn[kMultiMaxSlots], s_qe[kMultiMaxSlots];
+  __shared__ unsigned s_part[kBlock];
+  __shared__ int s_active;
+  InstDesc *I = P.inst;
+  const int ns = P.nslots;
+  const int t = threadIdx.x, lane = t & 31;
+  const long long tid = (long long)blockIdx.x * kBlock + t;
+  MultiCtl *ctl = P.ctl;
+
+  for (int i = t; i < ns; i += kBlock) s_d[i] = __ldcg(&I[i].d);
+  __syncthreads();
+
+  unsigned ph = 0;
+  for (; ph < (unsigned)P.max_phases; ++ph) {
+    /* ---- plan: identical in every CTA (reads counters finished before the
+     * last barrier) ---- */
+    if (t == 0) s_active = 0;
+    __syncthreads();
+    constexpr int kPer = (kMultiMaxSlots + kBlock - 1) / kBlock;
+    unsigned items[kPer];
+    unsigned sum = 0;
+    int act = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int i = t * kPer + j;
+      items[j] = 0;
+      if (i < ns) {
+        const int d = s_d[i];
+        const bool done = __ldcg(&I[i].done) != 0;
+        const unsigned long long qv = done ? 0ull : __ldcg(&I[i].ctr[d % 3]);
+        const unsigned qn = (unsigned)(qv >> 32), qe = (unsigned)qv;
+        s_qn[i] = qn;
+        s_qe[i] = qe;
+        if (qn) {
+          act = 1;
+          items[j] = (qe + kItemEdges - 1) / kItemEdges;
+        }
+        /* bookkeeping of the instance, by CTA 0 */
+        if (blockIdx.x == 0 && !done) {
+          if (qn) {
+            I[i].ctr[(d + 2) % 3] = 0ull;
+            I[i].levels = d + 1;
+            I[i].visited += qn;
+            I[i].edges += qe;
+          } else {
+            I[i].done = 1;
+          }
+        }
+      }
+      sum += items[j];
+    }
+    s_part[t] = sum;
+    if (act) s_active = 1;
+    __syncthreads();
+    /* exclusive scan of the per-thread sums */
+    for (int o = 1; o < kBlock; o <<= 1) {
+      const unsigned x = t >= o ? s_part[t - o] : 0u;
+      __syncthreads();
+      s_part[t] += x;
+      __syncthreads();
+    }
+    unsigned run = s_part[t] - sum;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int i = t * kPer + j;
+      if (i < ns) s_pre[i] = run;
+      run += items[j];
+    }
+    if (t == kBlock - 1) s_pre[ns] = s_part[t];
+    __syncthreads();
+    if (!s_active) break;
+    const unsigned total = s_pre[ns];
+    if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+
+    /* ---- claim items ---- */
+    for (;;) {
+      unsigned it = 0;
+      if (lane == 0) it = atomicAdd(&ctl->work[ph & 3u], 1u);
+      it = __shfl_sync(FULL, it, 0);
+      if (it >= total) break;
+      /* slot of the item: largest i with s_pre[i] <= it */
+      unsigned lo = 0, hi = (unsigned)ns;
+      while (hi - lo > 1) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (s_pre[mid] <= it)
+          lo = mid;
+        else
+          hi = mid;
+      }
+      const int i = (int)lo;
+      InstDesc &D = I[i];
+      const int d = s_d[i];
+      const unsigned qn = s_qn[i], qe = s_qe[i];
+      const int *q = D.q[d % 3];
+      const unsigned *e = D.e[d % 3];
+      int *qn_q = D.q[(d + 1) % 3];
+      unsigned *qn_e = D.e[(d + 1) % 3];
+      unsigned long long *ctr1 = &D.ctr[(d + 1) % 3];
+      const int *rp = D.rp, *jr = D.jr;
+      int *S = D.S;
+      unsigned long long *sig = D.sig;
+      const unsigned t0 = (it - s_pre[i]) * kItemEdges;
+      bool ovf = false;
+      for (int r = 0; r < kRounds; ++r) {
+        const unsigned tb = t0 + (unsigned)r * 32u;
+        if (tb >= qe) break;
+        /* owners: 32-ary search for the round's first edge, then a window of
+         * 32 queue entries searched with shuffles */
+        const unsigned o0 = dev::warp_find_owner(reinterpret_cast<const int *>(e), qn, tb);
+        const unsigned wi = o0 + lane;
+        const unsigned ew = wi < qn ? __ldcg(e + wi) : 0xffffffffu;
+        const unsigned tt = tb + lane;
+        unsigned j = 0;
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+          const unsigned ej = __shfl_sync(FULL, ew, (int)(j + s));
+          if (ej <= tt) j += s;
+        }
+        const unsigned elast = __shfl_sync(FULL, ew, 31);
+        bool claimed = false;
+        int v = 0;
+        unsigned dgo = 0;
+        if (tt < qe) {
+          unsigned o = o0 + j;
+          if (j == 31 && elast <= tt && o0 + 32 < qn) o = lane_owner(e, qn, tt); /* window too short */
+          const int u = __ldcg(q + o);
+          const unsigned off = tt - __ldcg(e + o);
+          v = __ldg(jr + __ldg(rp + u) + (int)off);
+          int sv = S[v];
+          if (sv == -1) {
+            sv = atomicCAS(S + v, -1, d + 1);
+            if (sv == -1) {
+              claimed = true;
+              sv = d + 1;
+              dgo = (unsigned)(__ldg(rp + v + 1) - __ldg(rp + v));
+            }
+          }
+          if (sig && sv == d + 1) {
+            const unsigned long long x = sig[u];
+            const unsigned long long old = atomicAdd(sig + v, x);
+            const unsigned long long s2 = old + x;
+            if (s2 < old || (s2 >> 63)) ovf = true;
+          }
+        }
+        enqueue(claimed, v, dgo, qn_q, qn_e, ctr1);
+      }
+      if (__any_sync(FULL, ovf) && lane == 0) atomicExch(&D.ovf, 1);
+    }
+    if (!grid_barrier(ctl, P.timeout_ns, (int)ph)) return;
+    for (int i = t; i < ns; i += kBlock)
+      if (s_qn[i]) s_d[i] += 1;
+    __syncthreads();
+  }
+  /* the level each instance runs next, for the following launch */
+  if (blockIdx.x == 0)
+    for (int i = t; i < ns; i += kBlock) I[i].d = s_d[i];
+  if (tid == 0) ctl->phases = (int)ph;
+}
+
+/* new instances: depth 0 and count 1 at the root, queue {root} */
+__global__ void multi_init_kernel(InstDesc *I, const int *slots, int k) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  InstDesc &D = I[slots[j]];
+  const int r = D.inv ? D.inv[D.root] : D.root;
+  D.S[r] = 0;
+  if (D.sig) D.sig[r] = 1ull;
+  D.q[0][0] = r;
+  D.e[0][0] = 0u;
+  D.ctr[0] = (1ull << 32) | (unsigned)(D.rp[r + 1] - D.rp[r]);
+}
+
+/* results in the caller's numbering: out[j] = S[inv[j]] */
+__global__ void multi_gather_kernel(const int *S, const unsigned long long *sig, const int *inv,
+                                    int n, int *S_out, unsigned long long *sig_out) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int v = inv ? inv[j] : (int)j;
+  S_out[j] = S[v];
+  if (sig_out) sig_out[j] = sig[v];
+}
+
+}  // namespace
+
+cudaError_t multi_geometry(int device, LaunchGeom *out) {
+  int sms = 0, coop = 0, per = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (e != cudaSuccess) return e;
+  if (!coop) return cudaErrorNotSupported;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, multi_bfs_kernel, kBlock, 0);
+  if (e != cudaSuccess) return e;
+  if (per < 1) return cudaErrorInvalidConfiguration;
+  out->block = kBlock;
+  out->grid = sms * per;
+  return cudaSuccess;
+}
+
+cudaError_t multi_launch(const MultiParams &p, const LaunchGeom &g, cudaStream_t s) {
+  void *args[] = {const_cast<MultiParams *>(&p)};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(multi_bfs_kernel), dim3(g.grid),
+                                     dim3(g.block), args, 0, s);
+}
+
+cudaError_t multi_init(InstDesc *inst, const int *slots, int k, cudaStream_t s) {
+  if (k <= 0) return cudaSuccess;
+  multi_init_kernel<<<(k + 127) / 128, 128, 0, s>>>(inst, slots, k);
+  return cudaGetLastError();
+}
+
+cudaError_t multi_gather(const int *S, const unsigned long long *sig, const int *inv, int n,
+                         int *S_out, unsigned long long *sig_out, cudaStream_t s) {
+  multi_gather_kernel<<<(unsigned)(((long long)n + 255) / 256), 256, 0, s>>>(S, sig, inv, n, S_out,
+                                                                            sig_out);
+  return cudaGetLastError();
+}
+
+}  // namespace tbfs

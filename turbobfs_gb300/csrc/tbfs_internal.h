@@ -163,6 +163,57 @@ cudaError_t batch_output(const BatchOutParams &o, bool sigma, cudaStream_t s);
 struct BatchWS; /* per-graph batch workspace (batch_api.cu) */
 void batch_ws_free(BatchWS *ws);
 
+/* ---- multi-instance engine (multi_engine.cu) ----
+ * One descriptor per traversal (graph, root); the kernel advances every
+ * unfinished descriptor by one level per phase. */
+constexpr int kMultiMaxSlots = 1024;
+
+struct InstDesc {
+  const int *cp, *ic;         /* in-lists  */
+  const int *rp, *jr;         /* out-lists (the pushes walk these) */
+  const int *inv;             /* caller id -> internal id, or null */
+  long long nnz;
+  int n;
+  int root;                   /* caller numbering */
+  int *S;                     /* n depths (internal numbering), -1 initially  */
+  unsigned long long *sig;    /* n path counts, 0 initially; null: depths only */
+  int *q[3];                  /* frontier queue of level d in q[d % 3] ...     */
+  unsigned *e[3];             /* ... with the exclusive prefix of out-degrees */
+  unsigned long long ctr[3];  /* queue of level d: (count << 32) | out-edges   */
+  int d;                      /* next level to run                             */
+  int done;                   /* 1: finished (or an empty slot)                */
+  int levels;
+  int ovf;                    /* a path count reached 2^63                     */
+  long long visited, edges;
+};
+
+struct __align__(128) MultiCtl {
+  unsigned work[4];
+  int status, timeout_level;
+  int phases;                 /* levels run by the launch */
+  int pad0[25];
+  unsigned bar_arrive;
+  unsigned pad1[31];
+  unsigned bar_gen;
+  unsigned pad2[31];
+};
+
+struct MultiParams {
+  InstDesc *inst;
+  int nslots;                 /* descriptors (<= kMultiMaxSlots) */
+  int max_phases;             /* stop after this many levels     */
+  MultiCtl *ctl;
+  long long timeout_ns;
+};
+
+cudaError_t multi_geometry(int device, LaunchGeom *out);
+cudaError_t multi_launch(const MultiParams &p, const LaunchGeom &g, cudaStream_t s);
+/* initialise the descriptors slots[0..k) (S = -1 and sig = 0 already set) */
+cudaError_t multi_init(InstDesc *inst, const int *slots, int k, cudaStream_t s);
+/* out[j] = S[inv[j]] (or S[j]) for j < n; sig likewise when sig_out is set */
+cudaError_t multi_gather(const int *S, const unsigned long long *sig, const int *inv, int n,
+                         int *S_out, unsigned long long *sig_out, cudaStream_t s);
+
 /* graph ingest helpers (graph_ingest.cu) */
 cudaError_t validate_csc(const int *cp, const int *ic, int n, long long nnz,
                          int *d_flag, cudaStream_t s);
