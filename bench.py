@@ -57,6 +57,16 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-threads", type=int, default=0)
+    p.add_argument("--no-batched", action="store_true", help="skip the batched report")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving report")
+    p.add_argument("--batch-scale", type=int, default=20)
+    p.add_argument("--batch-roots", type=int, default=256)
+    p.add_argument("--arena-graphs", type=int, default=512)
+    p.add_argument("--serving-graphs", type=int, default=64)
+    p.add_argument("--serving-max-scale", type=int, default=24)
+    p.add_argument("--serving-max-side", type=int, default=4096)
+    p.add_argument("--serving-rates", default="100,400,1600")
+    p.add_argument("--serving-queries", type=int, default=300)
     return p.parse_args()
 
 
@@ -326,6 +336,10 @@ def run_tbfs(args, world, rank, local):
         line["e2e"] = e2e
     if cb:
         line["cpu_baseline"] = cb
+    if rank == 0 and world == 1 and not args.no_batched:
+        line["batched"] = batched_report(args)
+    if rank == 0 and world == 1 and not args.no_serving:
+        line["serving"] = serving_report(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
@@ -390,6 +404,284 @@ def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
     finally:
         for b in bufs:
             L.tbfs_host_free_pinned(b)
+
+
+# ------------------------------------------------------------ batched ----
+
+def _event_ms(fn, reps=3, warm=3):
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def batched_report(args):
+    """C4: (a) k roots on one RMAT graph as one frontier-matrix launch
+    (tbfs_bfs_batch) against k back-to-back single-source traversals
+    (tbfs_bfs_many) of the same roots; (b) many mixed graphs in one packed
+    arena, one root each, in one launch (tbfs_arena_bfs) against one
+    single-source traversal per resident graph.  Device outputs, CUDA-event
+    timing on the legacy default stream both sides."""
+    import ctypes
+
+    import torch
+
+    import turbobfs_gb300 as tb
+    from turbobfs_gb300 import _lib, graphs
+    from turbobfs_gb300.api import _P_I32, _P_I64, make_options
+
+    L = tb.lib()
+    out = {}
+    # (a) frontier matrix
+    h = graphs.rmat(args.batch_scale, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    k = args.batch_roots
+    roots = np.ascontiguousarray(graphs.pick_roots(h, k, seed=1), dtype=np.int32)
+    n = h.n
+    with tb.Graph.from_host_csc(h) as g:
+        S = torch.empty((k, n), dtype=torch.int32, device="cuda")
+        sg = torch.empty((k, n), dtype=torch.int64, device="cuda")
+        st = (_lib.Stats * k)()
+        o = make_options("auto", True, outputs_on_device=True)
+
+        def batch():
+            _lib.check(L.tbfs_bfs_batch(g.handle, roots.ctypes.data_as(_P_I32), k, ctypes.byref(o),
+                                        _lib.LAYOUT_ROOT_MAJOR, S.data_ptr(), sg.data_ptr(), st),
+                       "tbfs_bfs_batch")
+
+        def plain():
+            _lib.check(L.tbfs_bfs_many(g.handle, roots.ctypes.data_as(_P_I32), k, ctypes.byref(o),
+                                       ctypes.cast(S.data_ptr(), _P_I32),
+                                       ctypes.cast(sg.data_ptr(), _P_I64), st), "tbfs_bfs_many")
+
+        t_plain = _event_ms(plain)
+        S_ref, sg_ref = S[::37].clone(), sg[::37].clone()
+        t_batch = _event_ms(batch)
+        same = bool(torch.equal(S[::37], S_ref) and torch.equal(sg[::37], sg_ref))
+        edges = sum(st[i].edges for i in range(k)) / 2
+        alg = sum(4 * st[i].edges + 8 * st[i].visited + 12 * n for i in range(k))
+        peak, peak_kind = measured_peak()
+        out["frontier_matrix"] = {
+            "workload": f"RMAT scale {args.batch_scale}, edgefactor 16, {k} roots in one launch, "
+                        "S int32 + sigma int64 (root-major, in HBM)",
+            "n": n, "nnz": h.nnz,
+            "batched_gteps": edges / t_batch / 1e6, "batched_ms": t_batch,
+            "plain_gteps": edges / t_plain / 1e6, "plain_ms": t_plain,
+            "speedup_vs_plain": t_plain / t_batch,
+            "launches": {"batched": (k + 255) // 256, "plain": k},
+            "results_identical_to_plain": same,
+            "roofline": {"bound": "hbm", "algorithmic_bytes": alg,
+                         "achieved_gbs": alg / (t_batch / 1e3) / 1e9,
+                         "frac": alg / (t_batch / 1e3) / 1e9 / peak,
+                         "peak": peak, "peak_source": f"{peak_kind} hbm_gbs",
+                         "note": "sum over roots of 4 nnz_c + 8 n_c + 12 n (per-root bytes; the "
+                                 "batch shares list reads, so this can exceed 1)"},
+        }
+        o2 = make_options("auto", False, outputs_on_device=True)
+
+        def batch_s():
+            _lib.check(L.tbfs_bfs_batch(g.handle, roots.ctypes.data_as(_P_I32), k, ctypes.byref(o2),
+                                        _lib.LAYOUT_ROOT_MAJOR, S.data_ptr(), None, st),
+                       "tbfs_bfs_batch")
+
+        def plain_s():
+            _lib.check(L.tbfs_bfs_many(g.handle, roots.ctypes.data_as(_P_I32), k, ctypes.byref(o2),
+                                       ctypes.cast(S.data_ptr(), _P_I32), None, st), "tbfs_bfs_many")
+
+        tb_s, tp_s = _event_ms(batch_s), _event_ms(plain_s)
+        out["frontier_matrix"]["depths_only"] = {
+            "batched_gteps": edges / tb_s / 1e6, "plain_gteps": edges / tp_s / 1e6,
+            "speedup_vs_plain": tp_s / tb_s}
+        del S, sg
+    # (b) packed arena of mixed graphs
+    if args.arena_graphs > 0:
+        rng = np.random.default_rng(5)
+        gs, kinds = [], []
+        for i in range(args.arena_graphs):
+            lg = float(rng.uniform(10, 20))
+            nv = int(2 ** lg)
+            kind = ("er", "rmat", "grid")[i % 3]
+            if kind == "er":
+                hh = graphs.erdos_renyi(nv, 4 * nv, seed=100 + i)
+            elif kind == "rmat":
+                hh = graphs.rmat(max(1, int(round(lg))), 16, seed=100 + i)
+            else:
+                hh = graphs.grid(max(2, int(round(nv ** 0.5))), seed=100 + i)
+            gs.append(hh)
+            kinds.append(kind)
+        aroots = np.array([int(graphs.pick_roots(hh, 1, seed=7)[0]) for hh in gs], dtype=np.int32)
+        arena = tb.Arena(gs)
+        tot = int(arena.offsets[-1])
+        S = torch.empty(tot, dtype=torch.int32, device="cuda")
+        sg = torch.empty(tot, dtype=torch.int64, device="cuda")
+        ast = (_lib.Stats * len(gs))()
+        oa = make_options("td", True, outputs_on_device=True)
+
+        def arena_run():
+            _lib.check(L.tbfs_arena_bfs(arena._h, aroots.ctypes.data_as(_P_I32), ctypes.byref(oa),
+                                        S.data_ptr(), sg.data_ptr(), ast), "tbfs_arena_bfs")
+
+        t_arena = _event_ms(arena_run)
+        a_edges = sum(ast[i].edges for i in range(len(gs))) / 2
+        a_levels = max(ast[i].levels for i in range(len(gs)))
+        resident = [tb.Graph.from_host_csc(hh) for hh in gs]
+        Sp = [torch.empty(hh.n, dtype=torch.int32, device="cuda") for hh in gs]
+        sgp = [torch.empty(hh.n, dtype=torch.int64, device="cuda") for hh in gs]
+        op = make_options("auto", True, outputs_on_device=True)
+        pst = _lib.Stats()
+
+        def plain_all():
+            for gi, gg in enumerate(resident):
+                _lib.check(L.tbfs_bfs(gg.handle, int(aroots[gi]), ctypes.byref(op),
+                                      ctypes.cast(Sp[gi].data_ptr(), _P_I32),
+                                      ctypes.cast(sgp[gi].data_ptr(), _P_I64), ctypes.byref(pst)),
+                           "tbfs_bfs")
+
+        t_plain_a = _event_ms(plain_all, reps=1, warm=1)
+        same = True
+        for gi in range(0, len(gs), 51):
+            lo = int(arena.offsets[gi])
+            same &= bool(torch.equal(S[lo:lo + gs[gi].n], Sp[gi]) and
+                         torch.equal(sg[lo:lo + gs[gi].n], sgp[gi]))
+        out["arena"] = {
+            "workload": f"{len(gs)} graphs (ER avg degree 8 / RMAT edgefactor 16 / 2D grid, "
+                        "n log-uniform in 2^10..2^20), one int32 offset arena, one root each "
+                        "(giant component), one launch",
+            "vertices": tot, "entries": int(arena.nnz.sum()), "max_levels": int(a_levels),
+            "arena_gteps": a_edges / t_arena / 1e6, "arena_ms": t_arena,
+            "plain_gteps": a_edges / t_plain_a / 1e6, "plain_ms": t_plain_a,
+            "plain_path": "one direction-optimizing tbfs_bfs per resident graph, back to back",
+            "speedup_vs_plain": t_plain_a / t_arena,
+            "results_identical_to_plain": same}
+        for gg in resident:
+            gg.close()
+        arena.close()
+        del S, sg, Sp, sgp
+    torch.cuda.empty_cache()
+    return out
+
+
+# ------------------------------------------------------------ serving ----
+
+def serving_graph_set(count, max_scale, max_side):
+    """count resident graphs: 5/8 RMAT (scales 12..max_scale, spread evenly,
+    the largest once each), 3/8 grids (sides log-spaced 64..max_side)."""
+    from turbobfs_gb300 import graphs
+
+    n_rmat = (count * 5) // 8
+    n_grid = count - n_rmat
+    scales = np.linspace(12, max_scale, n_rmat).round().astype(int)
+    sides = np.exp(np.linspace(np.log(64), np.log(max_side), n_grid)).round().astype(int)
+    hs = []
+    for i, sc in enumerate(scales):
+        hs.append(("rmat%d" % sc, graphs.rmat(int(sc), 16, seed=200 + i)))
+    for i, sd in enumerate(sides):
+        hs.append(("grid%d" % sd, graphs.grid(int(sd), seed=300 + i)))
+    return hs
+
+
+def serving_report(args):
+    """C5: Poisson arrivals of (graph, root) queries over resident graphs,
+    swept rate; the server (continuous batching) against the plain path
+    (one tbfs_bfs at a time, FIFO)."""
+    import turbobfs_gb300 as tb
+    from turbobfs_gb300 import graphs
+
+    t_gen = time.perf_counter()
+    hs = serving_graph_set(args.serving_graphs, args.serving_max_scale, args.serving_max_side)
+    t_gen = time.perf_counter() - t_gen
+    gs = [tb.Graph.from_host_csc(h) for _, h in hs]
+    hbm = sum(4 * (h.n + 1) + 4 * h.nnz for _, h in hs)
+    rng = np.random.default_rng(9)
+    nq = args.serving_queries
+    qg = rng.integers(0, len(gs), nq)
+    qr = []
+    for gi in qg:
+        h = hs[int(gi)][1]
+        # roots uniform over non-isolated vertices
+        deg = np.diff(h.col_ptr)
+        nz = np.flatnonzero(deg)
+        qr.append(int(nz[int(rng.integers(0, nz.size))]) if nz.size else 0)
+    # plain path: measured service time of every query, one at a time
+    svc, edges = [], []
+    for gi, r in zip(qg, qr):
+        gs[int(gi)].bfs(r)  # warm the graph's workspace
+    for gi, r in zip(qg, qr):
+        t0 = time.perf_counter()
+        res = gs[int(gi)].bfs(r)
+        svc.append(time.perf_counter() - t0)
+        edges.append(res.stats["edges"] / 2)
+    svc = np.array(svc)
+    edges_total = float(np.sum(edges))
+    rates = [float(x) for x in args.serving_rates.split(",") if x]
+    sweep = []
+    with tb.Server(max_slots=512, mem_budget=48 << 30) as srv:
+        for rate in rates:
+            gaps = rng.exponential(1.0 / rate, nq)
+            arrivals = np.cumsum(gaps)
+            # plain FIFO single server fed the same arrivals
+            fin, lat_p = 0.0, []
+            for a, sv in zip(arrivals, svc):
+                start = max(a, fin)
+                fin = start + sv
+                lat_p.append(fin - a)
+            plain_span = fin - arrivals[0]
+            # server: submit at the arrival times, wait for all
+            c0 = srv.counters()
+            tickets = []
+            t0 = time.perf_counter()
+            for a, gi, r in zip(arrivals, qg, qr):
+                now = time.perf_counter() - t0
+                if a > now:
+                    time.sleep(a - now)
+                tickets.append(srv.submit(gs[int(gi)], r))
+            lat_s = []
+            for tk in tickets:
+                _, lat = srv.wait(tk)
+                lat_s.append(lat)
+            span = time.perf_counter() - t0
+            c1 = srv.counters()
+            lat_s = np.array(lat_s)
+            lat_p = np.array(lat_p) * 1e3
+            sweep.append({
+                "rate_qps": rate, "queries": nq,
+                "server": {"p50_ms": float(np.percentile(lat_s, 50)),
+                           "p99_ms": float(np.percentile(lat_s, 99)),
+                           "gteps": edges_total / span / 1e9, "span_s": span,
+                           "launches": c1["launches"] - c0["launches"],
+                           "levels": c1["levels"] - c0["levels"]},
+                "plain_fifo": {"p50_ms": float(np.percentile(lat_p, 50)),
+                               "p99_ms": float(np.percentile(lat_p, 99)),
+                               "gteps": edges_total / plain_span / 1e9, "span_s": plain_span},
+            })
+    # results of the mix equal the plain results (spot check)
+    same = True
+    with tb.Server(max_slots=64, mem_budget=16 << 30) as srv:
+        sel = list(range(0, nq, max(1, nq // 24)))
+        tks = [srv.submit(gs[int(qg[i])], qr[i]) for i in sel]
+        for i, tk in zip(sel, tks):
+            res, _ = srv.wait(tk)
+            alone = gs[int(qg[i])].bfs(qr[i])
+            same &= bool(np.array_equal(res.S, alone.S) and np.array_equal(res.sigma, alone.sigma))
+    for g in gs:
+        g.close()
+    return {"workload": f"{len(hs)} resident graphs: {sum(1 for nm, _ in hs if nm.startswith('rmat'))} "
+                        f"RMAT (scales 12..{args.serving_max_scale}), "
+                        f"{sum(1 for nm, _ in hs if nm.startswith('grid'))} grids (sides 64..{args.serving_max_side}); "
+                        "(graph, root) uniform; Poisson arrivals; S + sigma copied to host per query",
+            "graph_bytes": hbm, "generation_s": t_gen,
+            "plain_mean_service_ms": float(svc.mean() * 1e3),
+            "sweep": sweep, "results_identical_to_plain": same,
+            "latency": "submit to results in host memory (server); FIFO replay of measured "
+                       "one-at-a-time service times on the same arrivals (plain)"}
 
 
 def main():

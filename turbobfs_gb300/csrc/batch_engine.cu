@@ -711,9 +711,19 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
                                  every thread, so every CTA takes the same
                                  direction) */
 
-  auto claim = [&](void) -> unsigned {
+  /* work items of a phase: the first one statically (global warp index),
+   * later ones from the phase's counter (after the static range) */
+  const unsigned nwarps = gridDim.x * kWarps;
+  const unsigned gwarp = blockIdx.x * kWarps + wid;
+  bool first_claim = true;
+  auto claim = [&](unsigned total) -> unsigned {
+    if (first_claim) {
+      first_claim = false;
+      return gwarp;
+    }
+    if (total <= nwarps) return 0xffffffffu; /* the static range covered all */
     unsigned it = 0;
-    if (g.lane == 0) it = atomicAdd(&ctl->work[ph & 3u], 1u);
+    if (g.lane == 0) it = nwarps + atomicAdd(&ctl->work[ph & 3u], 1u);
     return __shfl_sync(FULL, it, 0);
   };
   /* entries finished during level d go to slot (d + 1) % 4, read at the
@@ -782,8 +792,9 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
       /* ---- phase 1: discovery over the out-edges of Q_d ---- */
       const unsigned nA = (qe + kPushRounds * 32 - 1) / (kPushRounds * 32);
       if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+      first_claim = true;
       for (;;) {
-        const unsigned it = claim();
+        const unsigned it = claim(nA + nclear);
         if (it >= nA + nclear) break;
         if (it >= nA) {
           clear_item(it - nA);
@@ -848,8 +859,9 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
         return (long long)__ldcg(e1 + i) + (long long)kVCost * i;
       };
       if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+      first_claim = true;
       for (;;) {
-        const unsigned it = claim();
+        const unsigned it = claim(nA2 + nB2);
         if (it >= nA2 + nB2) break;
         if (it < nA2) {
           const unsigned is = warp_lower_bound(qcost, qn1, (long long)it * kItemCost);
@@ -895,8 +907,9 @@ __global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) 
         return (long long)__ldg(p.cp + v) + (long long)kVCost * v;
       };
       if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
+      first_claim = true;
       for (;;) {
-        const unsigned it = claim();
+        const unsigned it = claim(nA + nB + nclear);
         if (it >= nA + nB + nclear) break;
         if (it >= nA + nB) {
           clear_item(it - nA - nB);

@@ -576,14 +576,18 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     const unsigned n_a = A.pl.nch, n_ab = n_a + B.pl.nch, n_all = n_ab + n_tiles;
     unsigned *wctr = &ctl->work[d & 3];
     const int lane = threadIdx.x & 31;
-    for (;;) { /* dynamic scheduling: each warp claims the next work item */
-      unsigned item = 0;
-      if (lane == 0) item = atomicAdd(wctr, 1u);
-      item = __shfl_sync(FULL, item, 0);
-      if (item >= n_all) break;
+    /* work items: the first statically (global warp index), the rest from
+     * the level's counter past the static range, so that a small level
+     * costs no same-address atomics */
+    unsigned item = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    while (item < n_all) {
       if (item < n_a) run_expand_item(p, d, A, item, nx, bm_next, win, ovf);
       else if (item < n_ab) run_expand_item(p, d, B, item - n_a, nx, bm_next, win, ovf);
       else bu_tile(p, d, nx, bm_cur, bm_next, item - n_ab);
+      if (n_all <= nwarps) break;
+      unsigned nxt = 0;
+      if (lane == 0) nxt = nwarps + atomicAdd(wctr, 1u);
+      item = __shfl_sync(FULL, nxt, 0);
     }
     prev_qn = qn;
     prev_qe = qe;

@@ -326,6 +326,8 @@ extern "C" tbfs_status tbfs_arena_bfs(tbfs_arena *a, const int32_t *roots, const
     p.max_phases = INT32_MAX;
     p.ctl = a->ctl;
     p.timeout_ns = timeout;
+    p.wake = nullptr;
+    p.stop_on_done = 0;
     MTRY(cudaEventRecord(a->ev0, s), "event");
     MTRY(tbfs::multi_launch(p, a->geom, s), "multi launch");
     MTRY(cudaEventRecord(a->ev1, s), "event");
@@ -436,6 +438,9 @@ struct tbfs_server {
   MultiCtl *ctl = nullptr, *ctl_host = nullptr;
   LaunchGeom geom;
   cudaStream_t stream = nullptr;
+  /* set by submit, read by the running launch at every level boundary */
+  volatile int *wake_host = nullptr;
+  int *wake_dev = nullptr;
   /* request queue */
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -479,7 +484,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
         sv->cv_done.notify_all();
         continue;
       }
-      if (!sv->pool.alloc(need, &off)) break; /* wait for memory to free up */
+      if (!sv->pool.alloc(need, &off)) break; /* wait for memory to be released */
       Slot &sl = sv->slots[(size_t)free_slot];
       sl.busy = true;
       sl.req = r;
@@ -489,6 +494,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
       sv->pending.pop_front();
     }
     waiting = (int)sv->pending.size();
+    *sv->wake_host = 0; /* a submit from now on ends the next launch early */
   }
   cudaStream_t s = sv->stream;
   for (int i : admitted) {
@@ -527,14 +533,17 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
          "slots");
     MTRY(tbfs::multi_init(sv->inst, sv->slot_ids, (int)admitted.size(), s), "init");
   }
-  /* quantum: few levels while requests wait for a slot or memory, so that
-   * they are admitted soon; otherwise run long */
+  /* The launch runs until a query finishes (its results are delivered at
+   * once and its memory freed) or, unless queries already wait for memory
+   * or a slot, until a new query is submitted (it joins at the next level). */
   MultiParams p;
   p.inst = sv->inst;
   p.nslots = nslots;
-  p.max_phases = waiting > 0 ? 4 : 1 << 16;
+  p.max_phases = 1 << 20;
   p.ctl = sv->ctl;
   p.timeout_ns = sv->opt.timeout_ns > 0 ? sv->opt.timeout_ns : 4000000000LL;
+  p.wake = waiting > 0 ? nullptr : sv->wake_dev;
+  p.stop_on_done = 1;
   MTRY(cudaMemsetAsync(sv->ctl, 0, sizeof(MultiCtl), s), "clear control block");
   MTRY(tbfs::multi_launch(p, sv->geom, s), "multi launch");
   MTRY(cudaMemcpyAsync(sv->inst_host, sv->inst, (size_t)nslots * sizeof(InstDesc),
@@ -641,6 +650,7 @@ void server_free(tbfs_server *sv) {
   if (sv->inst_host) cudaFreeHost(sv->inst_host);
   if (sv->slot_ids_host) cudaFreeHost(sv->slot_ids_host);
   if (sv->ctl_host) cudaFreeHost(sv->ctl_host);
+  if (sv->wake_host) cudaFreeHost(const_cast<int *>(sv->wake_host));
   if (sv->stream) cudaStreamDestroy(sv->stream);
   delete sv;
 }
@@ -658,6 +668,11 @@ tbfs_status server_init(tbfs_server *sv) {
   MTRY(cudaMalloc(&sv->ctl, sizeof(MultiCtl)), "alloc");
   MTRY(cudaMallocHost(&sv->ctl_host, sizeof(MultiCtl)), "alloc");
   MTRY(tbfs::multi_geometry(sv->device, &sv->geom), "launch geometry");
+  int *wh = nullptr;
+  MTRY(cudaHostAlloc(&wh, sizeof(int), cudaHostAllocMapped), "wake flag");
+  sv->wake_host = wh;
+  *sv->wake_host = 0;
+  MTRY(cudaHostGetDevicePointer(&sv->wake_dev, wh, 0), "wake flag");
   sv->slots.assign((size_t)sv->max_slots, Slot());
   return TBFS_OK;
 }
@@ -723,6 +738,7 @@ extern "C" tbfs_status tbfs_server_submit(tbfs_server *sv, tbfs_graph *g, int32_
     r->ticket = sv->next_ticket++;
     sv->by_ticket[r->ticket] = r;
     sv->pending.push_back(r);
+    *sv->wake_host = 1;
   }
   sv->cv_work.notify_one();
   *ticket = r->ticket;

@@ -18,11 +18,13 @@
  *     edge or another) adds sigma[u] to sigma[v] with a 64-bit atomicAdd;
  *     sigma[u] is final because u was claimed a level earlier.
  * Work is edge-balanced across all instances: each CTA computes the same
- * prefix of per-instance work items (kItemEdges consecutive frontier
- * out-edges) in shared memory; a warp claims item indices from a global
- * counter and locates its instance by binary search in that prefix, the
- * owner of each edge by a 32-ary search over the instance's out-degree
- * prefix followed by a shuffle search in a 32-entry window.
+ * prefix of per-instance work items (rounds of 128 consecutive frontier
+ * out-edges, 4 per lane, with fewer rounds per item on small levels) in
+ * shared memory; a warp takes its first item by its global index and later
+ * ones from a counter, locates the instance by binary search in the prefix,
+ * and the owner of each edge by a 32-ary search over the instance's
+ * out-degree prefix (first round) followed by a shuffle search in a window
+ * of 64 queue entries.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -37,32 +39,48 @@ using dev::FULL;
 using dev::grid_barrier;
 
 constexpr int kBlock = 256;
-constexpr int kRounds = 8;                /* 32-edge rounds per item */
-constexpr unsigned kItemEdges = 32 * kRounds;
+constexpr int kEPT = 4;                   /* consecutive edges per lane per round */
+constexpr unsigned kRoundEdges = 32 * kEPT;
+constexpr int kMaxRounds = 8;             /* rounds per item, fewer on small levels */
 
-/* Append, for every lane with take set, (v, out-degree dg) to a queue:
- * one 64-bit atomic per warp reserves (count << 32 | edge sum).  All 32
+/* Append, for every lane and every bit j of take, (v[j], out-degree dg[j])
+ * to a queue: one 64-bit atomic per warp reserves (count << 32 | edge sum),
+ * so e[] stays the exclusive prefix of out-degrees in queue order.  All 32
  * lanes call. */
-__device__ __forceinline__ void enqueue(bool take, int v, unsigned dg, int *q, unsigned *e,
-                                        unsigned long long *ctr) {
+template <int N>
+__device__ __forceinline__ void enqueue_n(unsigned take, const int (&v)[N], const unsigned (&dg)[N],
+                                          int *q, unsigned *e, unsigned long long *ctr) {
   const int lane = threadIdx.x & 31;
-  const unsigned bal = __ballot_sync(FULL, take);
-  if (!bal) return;
-  const unsigned mine = take ? dg : 0u;
-  unsigned inc = mine;
+  if (!__any_sync(FULL, take != 0u)) return;
+  const unsigned cnt = __popc(take);
+  unsigned dsum = 0;
+#pragma unroll
+  for (int j = 0; j < N; ++j)
+    if ((take >> j) & 1u) dsum += dg[j];
+  unsigned ic = cnt, id = dsum;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const unsigned t = __shfl_up_sync(FULL, inc, o);
-    if (lane >= o) inc += t;
+    const unsigned tc = __shfl_up_sync(FULL, ic, o);
+    const unsigned td = __shfl_up_sync(FULL, id, o);
+    if (lane >= o) {
+      ic += tc;
+      id += td;
+    }
   }
-  const unsigned tot = __shfl_sync(FULL, inc, 31);
+  const unsigned tot_c = __shfl_sync(FULL, ic, 31), tot_d = __shfl_sync(FULL, id, 31);
   unsigned long long base = 0;
-  if (lane == 0) base = atomicAdd(ctr, ((unsigned long long)__popc(bal) << 32) | tot);
+  if (lane == 0) base = atomicAdd(ctr, ((unsigned long long)tot_c << 32) | tot_d);
   base = __shfl_sync(FULL, base, 0);
-  if (take) {
-    const unsigned pos = (unsigned)(base >> 32) + __popc(bal & ((1u << lane) - 1u));
-    q[pos] = v;
-    e[pos] = (unsigned)base + inc - mine;
+  unsigned pos = (unsigned)(base >> 32) + ic - cnt;
+  unsigned eo = (unsigned)base + id - dsum;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    if ((take >> j) & 1u) {
+      q[pos] = v[j];
+      e[pos] = eo;
+      ++pos;
+      eo += dg[j];
+    }
   }
 }
 
@@ -101,13 +119,13 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
     if (t == 0) s_active = 0;
     __syncthreads();
     constexpr int kPer = (kMultiMaxSlots + kBlock - 1) / kBlock;
-    unsigned items[kPer];
-    unsigned sum = 0;
-    int act = 0;
+    unsigned qes[kPer];
+    unsigned long long esum = 0;
+    int act = 0, fin = 0;
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
       const int i = t * kPer + j;
-      items[j] = 0;
+      qes[j] = 0;
       if (i < ns) {
         const int d = s_d[i];
         const bool done = __ldcg(&I[i].done) != 0;
@@ -117,7 +135,8 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
         s_qe[i] = qe;
         if (qn) {
           act = 1;
-          items[j] = (qe + kItemEdges - 1) / kItemEdges;
+          qes[j] = qe;
+          esum += qe;
         }
         /* bookkeeping of the instance, by CTA 0 */
         if (blockIdx.x == 0 && !done) {
@@ -128,13 +147,34 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
             I[i].edges += qe;
           } else {
             I[i].done = 1;
+            fin = 1;
           }
         }
       }
+    }
+    /* rounds per item: enough items for every warp on small levels */
+    s_part[t] = (unsigned)min(esum, 0xffffffffull);
+    if (act) s_active = 1;
+    if (fin && P.stop_on_done) ctl->stop = 1; /* CTA 0 only; read after the barrier */
+    __syncthreads();
+    for (int o = kBlock / 2; o > 0; o >>= 1) {
+      if (t < o) s_part[t] = (unsigned)min((unsigned long long)s_part[t] + s_part[t + o],
+                                           0xffffffffull);
+      __syncthreads();
+    }
+    const unsigned nwarps = gridDim.x * (kBlock / 32);
+    const unsigned long long per_warp = s_part[0] / ((unsigned long long)kRoundEdges * nwarps);
+    const unsigned rounds = (unsigned)max(1ull, min((unsigned long long)kMaxRounds, per_warp));
+    const unsigned iedges = kRoundEdges * rounds;
+    __syncthreads();
+    unsigned items[kPer];
+    unsigned sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      items[j] = (qes[j] + iedges - 1) / iedges;
       sum += items[j];
     }
     s_part[t] = sum;
-    if (act) s_active = 1;
     __syncthreads();
     /* exclusive scan of the per-thread sums */
     for (int o = 1; o < kBlock; o <<= 1) {
@@ -156,11 +196,11 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
     const unsigned total = s_pre[ns];
     if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
 
-    /* ---- claim items ---- */
-    for (;;) {
-      unsigned it = 0;
-      if (lane == 0) it = atomicAdd(&ctl->work[ph & 3u], 1u);
-      it = __shfl_sync(FULL, it, 0);
+    /* ---- claim items: the first one statically (global warp index), the
+     * rest from the phase's counter, so that a level with few items costs
+     * no same-address atomics ---- */
+    unsigned it = blockIdx.x * (kBlock / 32) + (t >> 5);
+    for (;; ) {
       if (it >= total) break;
       /* slot of the item: largest i with s_pre[i] <= it */
       unsigned lo = 0, hi = (unsigned)ns;
@@ -183,57 +223,97 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
       const int *rp = D.rp, *jr = D.jr;
       int *S = D.S;
       unsigned long long *sig = D.sig;
-      const unsigned t0 = (it - s_pre[i]) * kItemEdges;
+      const unsigned t0 = (it - s_pre[i]) * iedges;
       bool ovf = false;
-      for (int r = 0; r < kRounds; ++r) {
-        const unsigned tb = t0 + (unsigned)r * 32u;
+      unsigned o0 = 0xffffffffu; /* owner of the round's first edge, once known */
+      for (unsigned r = 0; r < rounds; ++r) {
+        const unsigned tb = t0 + r * kRoundEdges;
         if (tb >= qe) break;
-        /* owners: 32-ary search for the round's first edge, then a window of
-         * 32 queue entries searched with shuffles */
-        const unsigned o0 = dev::warp_find_owner(reinterpret_cast<const int *>(e), qn, tb);
+        /* owners: a 32-ary search for the item's first edge, afterwards the
+         * owner of the previous round's last edge; a window of 32 queue
+         * entries from there is searched with shuffles, edges beyond it
+         * (runs of empty lists) by a binary search of their own */
+        if (o0 == 0xffffffffu) o0 = dev::warp_find_owner(reinterpret_cast<const int *>(e), qn, tb);
         const unsigned wi = o0 + lane;
-        const unsigned ew = wi < qn ? __ldcg(e + wi) : 0xffffffffu;
-        const unsigned tt = tb + lane;
-        unsigned j = 0;
+        const unsigned ew0 = wi < qn ? __ldcg(e + wi) : 0xffffffffu;
+        const unsigned ew1 = wi + 32 < qn ? __ldcg(e + wi + 32) : 0xffffffffu;
+        const unsigned eend = o0 + 64 < qn ? __ldcg(e + o0 + 64) : 0xffffffffu;
+        unsigned tk[kEPT], oo[kEPT], off[kEPT];
 #pragma unroll
-        for (int s = 16; s > 0; s >>= 1) {
-          const unsigned ej = __shfl_sync(FULL, ew, (int)(j + s));
-          if (ej <= tt) j += s;
+        for (int k = 0; k < kEPT; ++k) {
+          tk[k] = tb + kEPT * lane + k;
+          unsigned j = 0; /* largest window index with e <= tk */
+#pragma unroll
+          for (int s = 32; s > 0; s >>= 1) {
+            const unsigned c = j + s;
+            const unsigned a0 = __shfl_sync(FULL, ew0, (int)(c & 31));
+            const unsigned a1 = __shfl_sync(FULL, ew1, (int)(c & 31));
+            if (c < 64 && (c < 32 ? a0 : a1) <= tk[k]) j = c;
+          }
+          const unsigned b0 = __shfl_sync(FULL, ew0, (int)(j & 31));
+          const unsigned b1 = __shfl_sync(FULL, ew1, (int)(j & 31));
+          const unsigned ej = j < 32 ? b0 : b1;
+          oo[k] = o0 + j;
+          off[k] = tk[k] - ej;
+          if (tk[k] < qe && tk[k] >= eend) {
+            oo[k] = lane_owner(e, qn, tk[k]);
+            off[k] = tk[k] - __ldcg(e + oo[k]);
+          }
         }
-        const unsigned elast = __shfl_sync(FULL, ew, 31);
-        bool claimed = false;
-        int v = 0;
-        unsigned dgo = 0;
-        if (tt < qe) {
-          unsigned o = o0 + j;
-          if (j == 31 && elast <= tt && o0 + 32 < qn) o = lane_owner(e, qn, tt); /* window too short */
-          const int u = __ldcg(q + o);
-          const unsigned off = tt - __ldcg(e + o);
-          v = __ldg(jr + __ldg(rp + u) + (int)off);
-          int sv = S[v];
-          if (sv == -1) {
-            sv = atomicCAS(S + v, -1, d + 1);
-            if (sv == -1) {
-              claimed = true;
-              sv = d + 1;
-              dgo = (unsigned)(__ldg(rp + v + 1) - __ldg(rp + v));
+        int u[kEPT], v[kEPT], sv[kEPT];
+        unsigned dgo[kEPT];
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k) u[k] = tk[k] < qe ? __ldcg(q + oo[k]) : 0;
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k)
+          v[k] = tk[k] < qe ? __ldg(jr + __ldg(rp + u[k]) + (int)off[k]) : 0;
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k) sv[k] = tk[k] < qe ? S[v[k]] : 0;
+        unsigned take = 0;
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k) {
+          dgo[k] = 0;
+          if (tk[k] < qe && sv[k] == -1) {
+            sv[k] = atomicCAS(S + v[k], -1, d + 1);
+            if (sv[k] == -1) {
+              take |= 1u << k;
+              sv[k] = d + 1;
             }
           }
-          if (sig && sv == d + 1) {
-            const unsigned long long x = sig[u];
-            const unsigned long long old = atomicAdd(sig + v, x);
-            const unsigned long long s2 = old + x;
-            if (s2 < old || (s2 >> 63)) ovf = true;
+        }
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k)
+          if ((take >> k) & 1u) dgo[k] = (unsigned)(__ldg(rp + v[k] + 1) - __ldg(rp + v[k]));
+        if (sig) {
+#pragma unroll
+          for (int k = 0; k < kEPT; ++k) {
+            if (tk[k] < qe && sv[k] == d + 1) {
+              const unsigned long long x = sig[u[k]];
+              const unsigned long long old = atomicAdd(sig + v[k], x);
+              const unsigned long long s2 = old + x;
+              if (s2 < old || (s2 >> 63)) ovf = true;
+            }
           }
         }
-        enqueue(claimed, v, dgo, qn_q, qn_e, ctr1);
+        enqueue_n<kEPT>(take, v, dgo, qn_q, qn_e, ctr1);
+        o0 = __shfl_sync(FULL, oo[kEPT - 1], 31); /* owner of the round's last edge */
       }
       if (__any_sync(FULL, ovf) && lane == 0) atomicExch(&D.ovf, 1);
+      if (total <= nwarps) break;
+      unsigned nx = 0;
+      if (lane == 0) nx = nwarps + atomicAdd(&ctl->work[ph & 3u], 1u);
+      it = __shfl_sync(FULL, nx, 0);
     }
+    /* a waiting request (host flag) ends the launch after this level */
+    if (tid == 0 && P.wake && *P.wake) ctl->stop = 1;
     if (!grid_barrier(ctl, P.timeout_ns, (int)ph)) return;
     for (int i = t; i < ns; i += kBlock)
       if (s_qn[i]) s_d[i] += 1;
     __syncthreads();
+    if (__ldcg(&ctl->stop)) {
+      ++ph;
+      break;
+    }
   }
   /* the level each instance runs next, for the following launch */
   if (blockIdx.x == 0)
@@ -276,6 +356,9 @@ cudaError_t multi_geometry(int device, LaunchGeom *out) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, multi_bfs_kernel, kBlock, 0);
   if (e != cudaSuccess) return e;
   if (per < 1) return cudaErrorInvalidConfiguration;
+  /* two CTAs (16 warps) per SM: enough to cover the latency of the pushes,
+   * and half the barrier arrivals of a fully occupied grid */
+  if (per > 2) per = 2;
   out->block = kBlock;
   out->grid = sms * per;
   return cudaSuccess;

@@ -191,7 +191,8 @@ struct __align__(128) MultiCtl {
   unsigned work[4];
   int status, timeout_level;
   int phases;                 /* levels run by the launch */
-  int pad0[25];
+  int stop;                   /* end the launch after the current level */
+  int pad0[24];
   unsigned bar_arrive;
   unsigned pad1[31];
   unsigned bar_gen;
@@ -204,6 +205,8 @@ struct MultiParams {
   int max_phases;             /* stop after this many levels     */
   MultiCtl *ctl;
   long long timeout_ns;
+  const volatile int *wake;   /* host-mapped flag: requests wait (null: none) */
+  int stop_on_done;           /* end the launch after a level that finished an instance */
 };
 
 cudaError_t multi_geometry(int device, LaunchGeom *out);
