@@ -181,10 +181,15 @@ void tbfs_arena_destroy(tbfs_arena *a);
  * and sigma[n] (sigma NULL: depths only), which must stay valid until
  * tbfs_server_wait(ticket) returns.  The loop admits queued queries into free
  * slots while the pool has room (about 48 n bytes per query with path
- * counts, 36 n without), runs one persistent launch that advances every
- * admitted query level by level -- a few levels at a time while queries are
- * waiting, so that they join soon, else to completion -- and retires the
- * finished ones.  Results equal tbfs_bfs's for the same (graph, root)
+ * counts, 32 n without), runs one persistent launch that advances every
+ * admitted query level by level -- until a query finishes or a new one is
+ * submitted, so that results leave and newcomers join at level
+ * boundaries -- and retires the finished ones.  Queries on large graphs
+ * (2^17 vertices or more) whose last traversal had at most 48 levels run
+ * instead, one at a time between those launches, on the single-source
+ * direction-optimizing engine (tbfs_bfs on the server's stream); callers
+ * must not traverse a served graph themselves while queries on it are
+ * pending.  Results equal tbfs_bfs's for the same (graph, root)
  * whatever else is running.  wait returns the query's status, statistics
  * and latency (submit to results in host memory, ms).  The graphs must
  * outlive their queries.  destroy fails queued queries, finishes running

@@ -171,3 +171,26 @@ def test_server_rejects_and_oversized(gpu_available, served_graphs):
         t2 = srv.submit(gs[4], 0, sigma=False)  # 5000 vertices, depths only: 160 KB, fits
         res, _ = srv.wait(t2)
         assert np.array_equal(res.S, gs[4].bfs(0, sigma=False).S)
+
+
+def test_server_routes_large_shallow_and_deep_graphs(gpu_available):
+    """RMAT scale 18 (2^18 vertices, ~6 levels) goes to the single-source
+    route; a 600x600 grid starts there (depth unknown) and moves to the
+    shared launches once its depth (over 48 levels) is known; small graphs
+    always share them.  Every result equals the query run alone."""
+    hs = [graphs.rmat(18, 16, seed=5), graphs.grid(600, seed=6), graphs.rmat(10, 16, seed=7)]
+    gs = [tb.Graph.from_host_csc(h) for h in hs]
+    try:
+        qs = [(i % 3, int(graphs.pick_roots(hs[i % 3], 1, seed=i)[0])) for i in range(18)]
+        with tb.Server(max_slots=16, mem_budget=2 << 30) as srv:
+            first = srv.wait(srv.submit(gs[1], qs[1][1]))  # learns the grid's depth
+            tickets = [srv.submit(gs[gi], r) for gi, r in qs]
+            results = [srv.wait(t) for t in tickets]
+        assert first[0].stats["levels"] > 48
+        for (gi, r), (res, _) in zip(qs, results):
+            alone = gs[gi].bfs(r)
+            assert np.array_equal(res.S, alone.S) and np.array_equal(res.sigma, alone.sigma)
+            assert res.stats["visited"] == alone.stats["visited"]
+    finally:
+        for g in gs:
+            g.close()

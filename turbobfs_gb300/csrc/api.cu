@@ -433,6 +433,7 @@ extern "C" tbfs_status tbfs_graph_last_stats(tbfs_graph *g, tbfs_stats *stats) {
     tbfs_stats st = {};
     tbfs_status s = stats_from(*g->ctl_host, g->ev0, g->ev1, &st);
     g->last = st;
+    g->depth_hint = st.levels;
     if (s != TBFS_OK) {
       *stats = st;
       return s;
@@ -532,6 +533,7 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
     st = stats_from(ctl_h[i], ev[2 * i], ev[2 * i + 1], &tmp);
     if (stats) stats[i] = tmp;
     g->last = tmp;
+    g->depth_hint = tmp.levels;
   }
   for (auto x : ev)
     if (x) cudaEventDestroy(x);

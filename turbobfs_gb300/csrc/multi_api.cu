@@ -370,6 +370,7 @@ struct Request {
   int32_t root = 0;
   int32_t *S = nullptr;
   int64_t *sigma = nullptr;
+  bool plain = false; /* served by the single-source engine */
   std::chrono::steady_clock::time_point t_submit;
   /* filled on completion */
   bool done = false;
@@ -445,17 +446,52 @@ struct tbfs_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Request>> pending;
+  std::deque<std::shared_ptr<Request>> plain_q; /* routed to the single-source engine */
   std::unordered_map<uint64_t, std::shared_ptr<Request>> by_ticket;
   uint64_t next_ticket = 1;
   bool stop = false;
   tbfs_status fatal = TBFS_OK;
   std::thread worker;
   /* counters */
-  long long launches = 0, levels_run = 0, completed = 0;
+  long long launches = 0, levels_run = 0, completed = 0, plain_runs = 0;
   double device_ms = 0.0;
 };
 
 namespace {
+
+/* Where a query runs.  Large graphs whose traversals are shallow (RMAT-like:
+ * few levels, huge frontiers) go to the single-source direction-optimizing
+ * engine, whose bottom-up levels beat the instances' top-down pushes there;
+ * everything else -- small graphs, and deep graphs whose levels are cheap but
+ * many -- shares the multi-instance launches.  The depth is that of the
+ * graph's last traversal (unknown before the first: then size decides). */
+constexpr int kPlainMinVertices = 1 << 17;
+constexpr int kPlainMaxLevels = 48;
+
+bool route_plain(const tbfs_graph *g) {
+  return g->n >= kPlainMinVertices && (g->depth_hint == 0 || g->depth_hint <= kPlainMaxLevels);
+}
+
+/* run one routed query to completion on the server's stream */
+void run_plain(tbfs_server *sv, const std::shared_ptr<Request> &r) {
+  tbfs_options o = sv->opt;
+  o.want_sigma = r->sigma != nullptr;
+  o.outputs_on_device = 0;
+  o.stream = sv->stream;
+  o.level_trace = nullptr;
+  o.level_trace_cap = 0;
+  tbfs_stats st = {};
+  const tbfs_status rc = tbfs_bfs(r->g, r->root, &o, r->S, r->sigma, &st);
+  const auto now = std::chrono::steady_clock::now();
+  std::lock_guard<std::mutex> lk(sv->mu);
+  r->stats = st;
+  r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
+  r->status = rc;
+  r->done = true;
+  sv->completed++;
+  sv->plain_runs++;
+  sv->cv_done.notify_all();
+}
 
 /* one step of the loop: admit, advance every instance up to max_phases
  * levels in one launch, retire the finished ones */
@@ -466,6 +502,12 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
     std::unique_lock<std::mutex> lk(sv->mu);
     while (!sv->pending.empty()) {
       auto &r = sv->pending.front();
+      if (route_plain(r->g)) {
+        r->plain = true;
+        sv->plain_q.push_back(r);
+        sv->pending.pop_front();
+        continue;
+      }
       const bool sigma = r->sigma != nullptr;
       const size_t need = inst_bytes(r->g->n, sigma) + align256((size_t)r->g->n * 4) +
                           (sigma ? align256((size_t)r->g->n * 8) : 0); /* + caller-order copy */
@@ -493,7 +535,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
       admitted.push_back(free_slot);
       sv->pending.pop_front();
     }
-    waiting = (int)sv->pending.size();
+    waiting = (int)(sv->pending.size() + sv->plain_q.size());
     *sv->wake_host = 0; /* a submit from now on ends the next launch early */
   }
   cudaStream_t s = sv->stream;
@@ -585,6 +627,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
     Slot &sl = sv->slots[(size_t)i];
     Request &r = *sl.req;
     fill_stats(sv->inst_host[i], 0.0f, &r.stats);
+    r.g->depth_hint = r.stats.levels;
     r.latency_ms = std::chrono::duration<double, std::milli>(now - r.t_submit).count();
     r.status = TBFS_OK;
     r.done = true;
@@ -604,21 +647,35 @@ void server_loop(tbfs_server *sv) {
       std::unique_lock<std::mutex> lk(sv->mu);
       bool any_busy = false;
       for (const Slot &sl : sv->slots) any_busy |= sl.busy;
-      sv->cv_work.wait(lk, [&] { return sv->stop || !sv->pending.empty() || any_busy; });
-      if (sv->stop && sv->pending.empty() && !any_busy) return;
+      sv->cv_work.wait(lk, [&] {
+        return sv->stop || !sv->pending.empty() || !sv->plain_q.empty() || any_busy;
+      });
+      if (sv->stop && sv->pending.empty() && sv->plain_q.empty() && !any_busy) return;
       if (sv->stop) {
         /* fail what is still queued, finish nothing new */
-        for (auto &r : sv->pending) {
-          r->status = TBFS_ERR_INVALID_ARG;
-          r->done = true;
-        }
+        for (auto *q : {&sv->pending, &sv->plain_q})
+          for (auto &r : *q) {
+            r->status = TBFS_ERR_INVALID_ARG;
+            r->done = true;
+          }
         sv->pending.clear();
+        sv->plain_q.clear();
         sv->cv_done.notify_all();
         if (!any_busy) return;
       }
     }
     bool idle = false;
-    const tbfs_status st = server_step(sv, &idle);
+    tbfs_status st = server_step(sv, &idle);
+    /* then one query of the single-source route, if any */
+    std::shared_ptr<Request> pr;
+    if (st == TBFS_OK) {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      if (!sv->plain_q.empty()) {
+        pr = sv->plain_q.front();
+        sv->plain_q.pop_front();
+      }
+    }
+    if (pr) run_plain(sv, pr);
     if (st != TBFS_OK) {
       std::lock_guard<std::mutex> lk(sv->mu);
       sv->fatal = st;
@@ -629,11 +686,13 @@ void server_loop(tbfs_server *sv) {
           sl.busy = false;
           sl.req.reset();
         }
-      for (auto &r : sv->pending) {
-        r->status = st;
-        r->done = true;
-      }
+      for (auto *q : {&sv->pending, &sv->plain_q})
+        for (auto &r : *q) {
+          r->status = st;
+          r->done = true;
+        }
       sv->pending.clear();
+      sv->plain_q.clear();
       sv->cv_done.notify_all();
       return;
     }

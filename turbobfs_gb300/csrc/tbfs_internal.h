@@ -264,6 +264,7 @@ struct tbfs_graph {
   cudaStream_t last_stream = nullptr;
   tbfs::LaunchGeom geom;
   tbfs::BatchWS *batch = nullptr; /* frontier-matrix workspace, on first use */
+  int depth_hint = 0; /* levels of the last traversal of this graph (0: none yet) */
   bool pending = false; /* a traversal was enqueued and not yet collected */
   tbfs_stats last = {};
 };
