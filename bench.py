@@ -57,6 +57,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-threads", type=int, default=0)
+    p.add_argument("--part", choices=["all", "batched", "serving"], default="all",
+                   help="batched / serving: run only that report and print it (profiling)")
     p.add_argument("--no-batched", action="store_true", help="skip the batched report")
     p.add_argument("--no-serving", action="store_true", help="skip the serving report")
     p.add_argument("--batch-scale", type=int, default=20)
@@ -235,6 +237,22 @@ def run_reference(args, world, rank):
     return 0
 
 
+def aggregate(t_ms: float, units: float, world: int, device="cpu"):
+    """Replicas: the slowest rank's time and the whole job's units (each rank
+    ran its own copy of the workload; nothing is exchanged on the data
+    path).  Returns (t_ms, units) unchanged for a single process."""
+    if world <= 1:
+        return float(t_ms), float(units)
+    import torch
+    import torch.distributed as dist
+
+    tt = torch.tensor([float(t_ms)], dtype=torch.float64, device=device)
+    uu = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    dist.all_reduce(uu, op=dist.ReduceOp.SUM)
+    return float(tt.item()), float(uu.item())
+
+
 def run_tbfs(args, world, rank, local):
     import torch
 
@@ -285,12 +303,7 @@ def run_tbfs(args, world, rank, local):
             launch_ms += [stats[i].device_ms for i in range(k)]
         e1.record()
         barrier()
-    t_ms = e0.elapsed_time(e1)
-    if world > 1:
-        tt = torch.tensor([t_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    units = world * args.steps * edges_per_step / 2
+    t_ms, units = aggregate(e0.elapsed_time(e1), args.steps * edges_per_step / 2, world, "cuda")
     value = units / (t_ms / 1e3) / 1e9
 
     # roofline of the persistent BFS kernel
@@ -689,6 +702,13 @@ def main():
     world, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.part != "all":
+        import torch
+
+        torch.cuda.set_device(local)
+        rep = batched_report(args) if args.part == "batched" else serving_report(args)
+        print(json.dumps({"part": args.part, args.part: rep}), flush=True)
+        return 0
     return run_tbfs(args, world, rank, local)
 
 
