@@ -151,6 +151,22 @@ tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
                            const tbfs_options *opt, int32_t layout, int32_t *S,
                            int64_t *sigma, tbfs_stats *stats);
 
+/* Betweenness centrality over the given roots: bc[v] = sum over roots s != v
+ * of Brandes' dependency delta_s(v) (U. Brandes, J. Math. Sociology 25(2),
+ * 2001), unnormalised; on an undirected graph every pair is counted in both
+ * directions (divide by 2 for the usual convention when all vertices are
+ * roots).  The forward phase is the engine's BFS (S, sigma); the dependency
+ * sweep pulls over out-lists level by level in a fixed summation order
+ * (below 32 entries in list order; otherwise strided by 32 and combined by
+ * a butterfly), with correctly rounded double operations, so results are
+ * reproducible bit for bit; the order of out-lists built on the device for
+ * a graph without TBFS_GRAPH_SYMMETRIC is not fixed, so there they agree to
+ * rounding.  bc (n doubles) is host or device memory per
+ * opt->outputs_on_device; *overflow (may be NULL) receives the number of
+ * roots whose path counts passed INT64_MAX (their ratios are then inexact). */
+tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t k, const tbfs_options *opt,
+                         double *bc, int32_t *overflow);
+
 /* ---- many graphs, one root each: a packed arena ----
  * No counterpart in the reference.  g graphs in one int32 offset arena:
  * graph i has n[i] vertices and nnz[i] CSC entries; col_ptr holds the g

@@ -42,6 +42,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_seq_csc_i32.argtypes = [_P_I32, _P_I32, _P_I32, _P_I32, c_int, c_int, c_int]
         L.oracle_seq_cooc_f32.argtypes = [_P_I32, _P_I32, _P_F32, c_int, c_int, c_int]
         L.oracle_exact_bfs.argtypes = [_P_I32, _P_I32, c_int, c_int, _P_I32, _P_I64, _P_U8]
+        L.oracle_brandes.argtypes = [_P_I32, _P_I32, c_int, _P_I32, c_int,
+                                     ctypes.POINTER(ctypes.c_double)]
         L.oracle_gpu_td_csc.argtypes = [_P_I32, _P_I32, _P_I32, _P_F32, c_int, c_int, c_int]
         L.oracle_gpu_bu_csc.argtypes = [_P_I32, _P_I32, _P_I32, c_int, c_int, c_int]
         L.oracle_gpu_tdbu_csc.argtypes = [_P_I32, _P_I32, _P_I32, _P_I32, c_int, c_int, c_int,
@@ -101,6 +103,18 @@ def exact_bfs(cp, ic, r):
     lv = lib().oracle_exact_bfs(_p(cp, _P_I32), _p(ic, _P_I32), n, r, _p(S, _P_I32),
                                 _p(sg, _P_I64), _p(ovf, _P_U8))
     return S, sg, ovf, lv
+
+
+def brandes(orp, ojr, roots):
+    """(bc float64[n], roots_with_wrapped_counts): betweenness over roots with
+    the GPU sweep's summation order; (orp, ojr) are the out-lists."""
+    orp, ojr = _i32(orp), _i32(ojr)
+    roots = _i32(roots)
+    n = orp.shape[0] - 1
+    bc = np.zeros(n, np.float64)
+    ovf = lib().oracle_brandes(_p(orp, _P_I32), _p(ojr, _P_I32), n, _p(roots, _P_I32),
+                               int(roots.shape[0]), bc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return bc, int(ovf)
 
 
 def gpu_td_csc(cp, ic, r):

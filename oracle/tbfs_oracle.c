@@ -497,3 +497,97 @@ double oracle_seq_many(const int *IC, const int *CP, int nz, int n,
   pthread_mutex_destroy(&c.mu);
   return t1 - t0;
 }
+
+
+/* ------------------------------------------------------------------
+ * Betweenness centrality (not in the reference: the dependency sweep of
+ * U. Brandes, J. Math. Sociology 25(2), 2001, on top of the reference's
+ * forward quantities S and sigma).  Restates the summation order of the
+ * library's GPU sweep so that results can be compared bit for bit:
+ * delta[v] sums sigma[v]/sigma[w] * (1 + delta[w]) over the out-list
+ * entries v -> w with S[w] = S[v] + 1; below 32 entries in list order,
+ * otherwise 32 strided partial sums (entries l, l+32, ...) combined by a
+ * butterfly (xor 16, 8, 4, 2, 1).  Built with -ffp-contract=off so that
+ * no multiply-add is fused.  (orp, ojr): out-lists; bc accumulates over
+ * the roots in order; returns the number of roots whose counts wrapped.
+ * ------------------------------------------------------------------ */
+int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int k, double *bc) {
+  int *S = (int *)malloc((size_t)n * sizeof(int));
+  uint64_t *sg = (uint64_t *)malloc((size_t)n * sizeof(uint64_t));
+  int *q = (int *)malloc((size_t)n * sizeof(int));
+  double *delta = (double *)malloc((size_t)n * sizeof(double));
+  int ovf_roots = 0;
+  memset(bc, 0, (size_t)n * sizeof(double));
+  for (int ri = 0; ri < k; ++ri) {
+    const int r = roots[ri];
+    for (int v = 0; v < n; ++v) {
+      S[v] = -1;
+      sg[v] = 0;
+      delta[v] = 0.0;
+    }
+    int head = 0, tail = 0, ovf = 0;
+    S[r] = 0;
+    sg[r] = 1;
+    q[tail++] = r;
+    while (head < tail) { /* queue order = depth order */
+      const int u = q[head++];
+      for (int e = orp[u]; e < orp[u + 1]; ++e) {
+        const int w = ojr[e];
+        if (S[w] < 0) {
+          S[w] = S[u] + 1;
+          q[tail++] = w;
+        }
+        if (S[w] == S[u] + 1) {
+          const uint64_t t = sg[w] + sg[u];
+          if (t < sg[w] || (t >> 63)) ovf = 1;
+          sg[w] = t;
+        }
+      }
+    }
+    ovf_roots += ovf;
+    for (int i = tail - 1; i >= 0; --i) { /* deepest first */
+      const int v = q[i];
+      const int d = S[v], b = orp[v], e = orp[v + 1];
+      const double sv = (double)sg[v];
+      double acc = 0.0;
+      if (e - b < 32) {
+        for (int j = b; j < e; ++j) {
+          const int w = ojr[j];
+          if (S[w] == d + 1) {
+            const double c = sv / (double)sg[w];
+            const double t = 1.0 + delta[w];
+            const double term = c * t;
+            acc = acc + term;
+          }
+        }
+      } else {
+        double part[32], nxt[32];
+        for (int l = 0; l < 32; ++l) {
+          double a = 0.0;
+          for (int j = b + l; j < e; j += 32) {
+            const int w = ojr[j];
+            if (S[w] == d + 1) {
+              const double c = sv / (double)sg[w];
+              const double t = 1.0 + delta[w];
+              const double term = c * t;
+              a = a + term;
+            }
+          }
+          part[l] = a;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          for (int l = 0; l < 32; ++l) nxt[l] = part[l] + part[l ^ o];
+          memcpy(part, nxt, sizeof(part));
+        }
+        acc = part[0];
+      }
+      delta[v] = acc;
+      if (v != r) bc[v] = bc[v] + acc;
+    }
+  }
+  free(S);
+  free(sg);
+  free(q);
+  free(delta);
+  return ovf_roots;
+}

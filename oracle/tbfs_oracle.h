@@ -72,6 +72,9 @@ double oracle_seq_many(const int *IC, const int *CP, int nz, int n,
                        const int *roots, int k, int threads, double *seconds,
                        int64_t *edges);
 
+/* Brandes betweenness with the GPU sweep's summation order (see .c) */
+int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int k, double *bc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,6 +91,8 @@ _SIGNATURES = {
                               POINTER(Stats)]),
     "tbfs_bfs_batch": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_int32, c_void_p,
                                c_void_p, POINTER(Stats)]),
+    "tbfs_brandes": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_void_p,
+                             POINTER(c_int32)]),
     "tbfs_arena_create": (c_int, [c_int32, _P_I32, _P_I64, _P_I32, _P_I32, c_uint32,
                                   POINTER(c_void_p)]),
     "tbfs_arena_info": (c_int, [c_void_p, _P_I32, _P_I64, _P_I64]),

@@ -184,6 +184,19 @@ class Graph:
             out[0]["trace"], out[0]["trace_end_us"] = _parse_trace(tr)
         return S, sg, out
 
+    def betweenness(self, roots=None, **kw):
+        """Brandes betweenness over ``roots`` (default: every vertex):
+        (bc float64[n], number of roots whose path counts overflowed).
+        Unnormalised; an undirected graph counts every pair from both ends."""
+        roots = _i32(np.arange(self.n) if roots is None else roots)
+        o = make_options("auto", True, **kw)
+        bc = np.zeros(self.n, dtype=np.float64)
+        ovf = ctypes.c_int32()
+        check(lib().tbfs_brandes(self.handle, _ptr(roots, _P_I32), int(roots.shape[0]),
+                                 ctypes.byref(o), bc.ctypes.data, ctypes.byref(ovf)),
+              "tbfs_brandes")
+        return bc, int(ovf.value)
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
             lib().tbfs_graph_destroy(self._h)

@@ -397,6 +397,19 @@ static tbfs_status enqueue_bfs(tbfs_graph *g, const BfsParams &p, cudaStream_t s
   return TBFS_OK;
 }
 
+/* forward traversal with S / sigma left in the graph's internal numbering
+ * (device arrays of n), for consumers inside the library */
+tbfs_status tbfs::forward_internal(tbfs_graph *g, int32_t root, const tbfs_options &o, int *S,
+                                   unsigned long long *sigma, cudaStream_t s, BfsCtl *ctl_host) {
+  BfsParams p = make_params(g, root, o, S, sigma);
+  p.S = S;
+  p.sigma = o.want_sigma ? sigma : nullptr;
+  p.S_out = S;
+  p.sigma_out = p.sigma;
+  p.perm = nullptr; /* no scatter into the caller's order; inv still maps the root */
+  return enqueue_bfs(g, p, s, g->ev0, g->ev1, ctl_host);
+}
+
 static tbfs_status stats_from(const BfsCtl &c, cudaEvent_t ev0, cudaEvent_t ev1,
                               tbfs_stats *st) {
   float ms = 0.0f;

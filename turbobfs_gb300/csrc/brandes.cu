@@ -1,0 +1,357 @@
+/*
+ * brandes.cu -- betweenness centrality: the forward traversal of the engine
+ * (depths S and path counts sigma, exactly what the reference computes) plus
+ * Brandes' dependency sweep (U. Brandes, "A faster algorithm for betweenness
+ * centrality", J. Math. Sociology 25(2), 2001):
+ *
+ *   delta[v] = sum over out-list entries v -> w with S[w] = S[v] + 1 of
+ *              sigma[v] / sigma[w] * (1 + delta[w]),
+ *   bc[v]   += delta[v] for every root s != v.
+ *
+ * The sweep runs level by level from the deepest level up, as one
+ * persistent cooperative launch per root with a grid barrier between levels.
+ * Vertices are grouped by depth with a block-aggregated counting sort.
+ * Every delta is a pull over the vertex's own out-list in a fixed order, so
+ * the result does not depend on scheduling:
+ *   out-degree < 32: one lane sums the terms in list order;
+ *   otherwise: lane l sums the entries l, l+32, l+64, ... in order, then the
+ *   32 partial sums meet in a butterfly (xor 16, 8, 4, 2, 1).
+ * Terms are (double)sigma[v] / (double)sigma[w] * (1 + delta[w]) with
+ * correctly rounded IEEE operations and no contraction into fused
+ * multiply-adds, so a CPU restatement of the same order reproduces every
+ * bit.  bc accumulates the roots in the order given.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "device_common.cuh"
+#include "tbfs.h"
+#include "tbfs_internal.h"
+
+namespace tbfs {
+namespace {
+
+using dev::FULL;
+using dev::grid_barrier;
+
+constexpr int kBlock = 256;
+constexpr int kSmemLevels = 8192; /* levels counted in shared memory per block */
+constexpr int kTile = 4096;       /* vertices per block of the counting sort   */
+constexpr int kWarpDegree = 32;   /* out-degree from which a warp sums a vertex */
+
+struct __align__(128) SweepCtl {
+  int status, timeout_level;
+  int pad0[30];
+  unsigned bar_arrive;
+  unsigned pad1[31];
+  unsigned bar_gen;
+  unsigned pad2[31];
+};
+
+struct SweepParams {
+  const int *rp, *jr;                /* out-lists (internal numbering)       */
+  const int *S;                      /* depths of the forward traversal      */
+  const unsigned long long *sig;     /* path counts                          */
+  const int *list;                   /* vertices grouped by depth ...        */
+  const int *off;                    /* ... level d at list[off[d], off[d+1]) */
+  int levels;
+  int root;                          /* caller numbering ...                 */
+  const int *inv;                    /* ... mapped by inv (or null)          */
+  double *delta;                     /* n, zero on entry                     */
+  double *bc;                        /* n, accumulated                       */
+  SweepCtl *ctl;
+  long long timeout_ns;
+};
+
+__device__ __forceinline__ double term(const SweepParams &p, double sv, int w) {
+  const double sw = (double)__ldg(p.sig + w);
+  return __dmul_rn(__ddiv_rn(sv, sw), __dadd_rn(1.0, __ldcg(p.delta + w)));
+}
+
+/* acc += the terms of entries k0, k0 + step, ... < e, in that order; four
+ * entries' loads are issued before their terms are added */
+__device__ __forceinline__ double sum_entries(const SweepParams &p, int d, double sv, int k0,
+                                              int e, int step) {
+  double acc = 0.0;
+  int k = k0;
+  for (; k + 3 * step < e; k += 4 * step) {
+    int w[4];
+    bool c[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) w[j] = __ldg(p.jr + k + j * step);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) c[j] = __ldg(p.S + w[j]) == d + 1;
+    double t[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) t[j] = c[j] ? term(p, sv, w[j]) : 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (c[j]) acc = __dadd_rn(acc, t[j]);
+  }
+  for (; k < e; k += step) {
+    const int w = __ldg(p.jr + k);
+    if (__ldg(p.S + w) == d + 1) acc = __dadd_rn(acc, term(p, sv, w));
+  }
+  return acc;
+}
+
+__global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
+  const int lane = threadIdx.x & 31;
+  const int root = p.inv ? __ldg(p.inv + p.root) : p.root;
+  const unsigned gwarp = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const unsigned nwarps = (gridDim.x * kBlock) >> 5;
+  for (int d = p.levels - 2; d >= 0; --d) {
+    const int lo = __ldg(p.off + d), hi = __ldg(p.off + d + 1);
+    /* chunks of 32 vertices of level d per warp */
+    for (int base = lo + (int)gwarp * 32; base < hi; base += (int)nwarps * 32) {
+      const int i = base + lane;
+      int v = -1, b = 0, e = 0;
+      if (i < hi) {
+        v = __ldg(p.list + i);
+        b = __ldg(p.rp + v);
+        e = __ldg(p.rp + v + 1);
+      }
+      const bool heavy = v >= 0 && e - b >= kWarpDegree;
+      if (v >= 0 && !heavy) {
+        const double acc = sum_entries(p, d, (double)__ldg(p.sig + v), b, e, 1);
+        p.delta[v] = acc;
+        if (v != root) p.bc[v] = __dadd_rn(p.bc[v], acc);
+      }
+      /* heavy vertices of the chunk, one at a time with the whole warp */
+      unsigned hv = __ballot_sync(FULL, heavy);
+      while (hv) {
+        const int src = __ffs(hv) - 1;
+        hv &= hv - 1u;
+        const int vv = __shfl_sync(FULL, v, src);
+        const int bb = __shfl_sync(FULL, b, src), ee = __shfl_sync(FULL, e, src);
+        double acc = sum_entries(p, d, (double)__ldg(p.sig + vv), bb + lane, ee, 32);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(FULL, acc, o));
+        if (lane == 0) {
+          p.delta[vv] = acc;
+          if (vv != root) p.bc[vv] = __dadd_rn(p.bc[vv], acc);
+        }
+      }
+    }
+    if (!grid_barrier(p.ctl, p.timeout_ns, d)) return;
+  }
+}
+
+/* ---- vertices grouped by depth (counting sort, block-aggregated) ---- */
+
+/* counts[d] = vertices at depth d */
+__global__ void level_count_kernel(const int *S, int n, int levels, int *counts) {
+  __shared__ int h[kSmemLevels];
+  const bool local = levels <= kSmemLevels;
+  if (local)
+    for (int d = threadIdx.x; d < levels; d += blockDim.x) h[d] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kTile;
+  for (int j = threadIdx.x; j < kTile; j += blockDim.x) {
+    const long long v = base + j;
+    if (v >= n) break;
+    const int d = S[v];
+    if (d < 0) continue;
+    if (local)
+      atomicAdd(&h[d], 1);
+    else
+      atomicAdd(&counts[d], 1);
+  }
+  __syncthreads();
+  if (local)
+    for (int d = threadIdx.x; d < levels; d += blockDim.x)
+      if (h[d]) atomicAdd(&counts[d], h[d]);
+}
+
+/* list[...] = vertices by depth; fill[d] starts at the exclusive prefix */
+__global__ void level_fill_kernel(const int *S, int n, int levels, int *fill, int *list) {
+  __shared__ int h[kSmemLevels];
+  const bool local = levels <= kSmemLevels;
+  if (local)
+    for (int d = threadIdx.x; d < levels; d += blockDim.x) h[d] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kTile;
+  if (local) {
+    for (int j = threadIdx.x; j < kTile; j += blockDim.x) {
+      const long long v = base + j;
+      if (v >= n) break;
+      const int d = S[v];
+      if (d >= 0) atomicAdd(&h[d], 1);
+    }
+    __syncthreads();
+    /* reserve this block's range of every level, then hand out positions */
+    for (int d = threadIdx.x; d < levels; d += blockDim.x)
+      if (h[d]) h[d] = atomicAdd(&fill[d], h[d]);
+    __syncthreads();
+    for (int j = threadIdx.x; j < kTile; j += blockDim.x) {
+      const long long v = base + j;
+      if (v >= n) break;
+      const int d = S[v];
+      if (d >= 0) list[atomicAdd(&h[d], 1)] = (int)v;
+    }
+  } else {
+    for (int j = threadIdx.x; j < kTile; j += blockDim.x) {
+      const long long v = base + j;
+      if (v >= n) break;
+      const int d = S[v];
+      if (d >= 0) list[atomicAdd(&fill[d], 1)] = (int)v;
+    }
+  }
+}
+
+/* out[j] = in[inv[j]] (or in[j]) */
+__global__ void gather_double_kernel(const double *in, const int *inv, int n, double *out) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) out[j] = in[inv ? inv[j] : j];
+}
+
+}  // namespace
+}  // namespace tbfs
+
+using tbfs::SweepCtl;
+using tbfs::SweepParams;
+
+namespace {
+
+tbfs_status bfail(cudaError_t e, const char *what) {
+  tbfs_set_error("tbfs_brandes: %s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? TBFS_ERR_OUT_OF_MEMORY : TBFS_ERR_CUDA;
+}
+
+#define BTRY(call, what)                            \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return bfail(e_, what);  \
+  } while (0)
+
+struct Scratch {
+  int *S = nullptr, *list = nullptr, *off = nullptr, *fill = nullptr;
+  unsigned long long *sig = nullptr;
+  double *delta = nullptr, *bc = nullptr, *out = nullptr;
+  SweepCtl *ctl = nullptr;
+  tbfs::BfsCtl *fctl_host = nullptr;
+  SweepCtl *ctl_host = nullptr;
+  ~Scratch() {
+    cudaFree(S);
+    cudaFree(list);
+    cudaFree(off);
+    cudaFree(fill);
+    cudaFree(sig);
+    cudaFree(delta);
+    cudaFree(bc);
+    cudaFree(out);
+    cudaFree(ctl);
+    if (fctl_host) cudaFreeHost(fctl_host);
+    if (ctl_host) cudaFreeHost(ctl_host);
+  }
+};
+
+}  // namespace
+
+extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t k,
+                                    const tbfs_options *opt, double *bc, int32_t *overflow) {
+  tbfs_options o;
+  tbfs_options_init(&o);
+  if (opt) o = *opt;
+  if (!g || k < 0 || (k > 0 && !roots) || !bc) {
+    tbfs_set_error("tbfs_brandes: null graph, roots or bc, or k < 0");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  for (int32_t i = 0; i < k; ++i)
+    if (roots[i] < 0 || roots[i] >= g->n) {
+      tbfs_set_error("tbfs_brandes: root %d (index %d) outside [0, n)", roots[i], i);
+      return TBFS_ERR_INVALID_ARG;
+    }
+  BTRY(cudaSetDevice(g->device), "cudaSetDevice");
+  cudaStream_t s = (cudaStream_t)o.stream;
+  const size_t n = (size_t)g->n;
+  Scratch w;
+  BTRY(cudaMalloc(&w.S, n * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.sig, n * sizeof(unsigned long long)), "alloc");
+  BTRY(cudaMalloc(&w.list, n * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.off, (n + 2) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.fill, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.delta, n * sizeof(double)), "alloc");
+  BTRY(cudaMalloc(&w.bc, n * sizeof(double)), "alloc");
+  BTRY(cudaMalloc(&w.ctl, sizeof(SweepCtl)), "alloc");
+  BTRY(cudaMallocHost(&w.fctl_host, sizeof(tbfs::BfsCtl)), "alloc");
+  BTRY(cudaMemsetAsync(w.bc, 0, n * sizeof(double), s), "clear");
+  /* grid of the sweep: all SMs, as occupancy allows (cooperative) */
+  int sms = 0, per = 0;
+  BTRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device), "attribute");
+  BTRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tbfs::sweep_kernel, tbfs::kBlock, 0),
+       "occupancy");
+  if (per > 2) per = 2;
+  const unsigned grid = (unsigned)(sms * (per > 0 ? per : 1));
+  const unsigned tiles = (unsigned)((n + tbfs::kTile - 1) / tbfs::kTile);
+  const long long timeout = o.timeout_ns > 0 ? o.timeout_ns : 4000000000LL;
+  int32_t ovf_roots = 0;
+  tbfs_options fo = o;
+  fo.want_sigma = 1;
+  fo.outputs_on_device = 1;
+  fo.level_trace = nullptr;
+  fo.level_trace_cap = 0;
+  for (int32_t r = 0; r < k; ++r) {
+    tbfs_status st = tbfs::forward_internal(g, roots[r], fo, w.S, w.sig, s, w.fctl_host);
+    if (st != TBFS_OK) return st;
+    BTRY(cudaStreamSynchronize(s), "forward traversal");
+    const tbfs::BfsCtl &fc = *w.fctl_host;
+    if (fc.status != 0) {
+      tbfs_set_error("tbfs_brandes: forward traversal: grid barrier wait exceeded its budget");
+      return TBFS_ERR_TIMEOUT;
+    }
+    if (fc.sigma_overflow) ++ovf_roots;
+    const int levels = fc.levels;
+    if (levels < 2) continue; /* an isolated root: no dependencies */
+    /* vertices by depth */
+    BTRY(cudaMemsetAsync(w.off, 0, ((size_t)levels + 1) * sizeof(int), s), "clear");
+    tbfs::level_count_kernel<<<tiles, tbfs::kBlock, 0, s>>>(w.S, g->n, levels, w.off);
+    BTRY(cudaGetLastError(), "level count");
+    BTRY(tbfs::exclusive_scan(w.off, (long long)levels + 1, w.off, s), "level prefix");
+    BTRY(cudaMemcpyAsync(w.fill, w.off, (size_t)levels * sizeof(int), cudaMemcpyDeviceToDevice, s),
+         "fill pointers");
+    tbfs::level_fill_kernel<<<tiles, tbfs::kBlock, 0, s>>>(w.S, g->n, levels, w.fill, w.list);
+    BTRY(cudaGetLastError(), "level fill");
+    BTRY(cudaMemsetAsync(w.delta, 0, n * sizeof(double), s), "clear");
+    BTRY(cudaMemsetAsync(w.ctl, 0, sizeof(SweepCtl), s), "clear");
+    SweepParams p;
+    p.rp = g->rp;
+    p.jr = g->jr;
+    p.S = w.S;
+    p.sig = w.sig;
+    p.list = w.list;
+    p.off = w.off;
+    p.levels = levels;
+    p.root = roots[r];
+    p.inv = g->inv;
+    p.delta = w.delta;
+    p.bc = w.bc;
+    p.ctl = w.ctl;
+    p.timeout_ns = timeout;
+    void *args[] = {&p};
+    BTRY(cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(tbfs::sweep_kernel), dim3(grid),
+                                     dim3(tbfs::kBlock), args, 0, s),
+         "dependency sweep");
+    BTRY(cudaStreamSynchronize(s), "dependency sweep");
+    SweepCtl sc;
+    BTRY(cudaMemcpy(&sc, w.ctl, sizeof(sc), cudaMemcpyDeviceToHost), "read sweep status");
+    if (sc.status != 0) {
+      tbfs_set_error("tbfs_brandes: sweep: grid barrier wait exceeded its budget");
+      return TBFS_ERR_TIMEOUT;
+    }
+  }
+  /* results in the caller's numbering */
+  double *dst = bc;
+  if (!o.outputs_on_device) {
+    BTRY(cudaMalloc(&w.out, n * sizeof(double)), "alloc");
+    dst = w.out;
+  }
+  tbfs::gather_double_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w.bc, g->inv, g->n, dst);
+  BTRY(cudaGetLastError(), "gather");
+  if (!o.outputs_on_device)
+    BTRY(cudaMemcpyAsync(bc, w.out, n * sizeof(double), cudaMemcpyDeviceToHost, s), "copy bc");
+  BTRY(cudaStreamSynchronize(s), "results");
+  if (overflow) *overflow = ovf_roots;
+  return TBFS_OK;
+}

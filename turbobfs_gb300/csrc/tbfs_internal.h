@@ -269,6 +269,12 @@ struct tbfs_graph {
   tbfs_stats last = {};
 };
 
+namespace tbfs {
+/* one traversal with results in the internal numbering (api.cu) */
+tbfs_status forward_internal(tbfs_graph *g, int32_t root, const tbfs_options &o, int *S,
+                             unsigned long long *sigma, cudaStream_t s, BfsCtl *ctl_host);
+}  // namespace tbfs
+
 extern "C" void tbfs_set_error(const char *fmt, ...);
 
 #endif
