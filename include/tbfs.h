@@ -151,6 +151,24 @@ tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
                            const tbfs_options *opt, int32_t layout, int32_t *S,
                            int64_t *sigma, tbfs_stats *stats);
 
+/* Degree profile of a resident graph, computed on the device: hist40[b] =
+ * vertices whose in-degree d has floor(log2(d+1)) == b (b < 40), the maximum
+ * and the mean in-degree (the statistics of the reference's degree.c:22-141;
+ * the same definition as tbfs_degree_profile of tbfs_graphgen.h on a host
+ * CSC).  max_degree and mean_degree may be NULL. */
+tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40, int64_t *max_degree,
+                                      double *mean_degree);
+
+/* Autotuner: picks alpha, beta and pull_ratio for g by timing traversals
+ * from the k sample roots (device events; each parameter in turn over a
+ * short candidate list, starting from opt's values' defaults) and writes
+ * them into *opt, leaving its other fields as they are.  With cache_path
+ * (a text file; NULL: no cache) the result is stored under a key made of
+ * the graph's degree-profile shape, and a later call on a graph with the
+ * same key returns the stored values without timing (*from_cache = 1). */
+tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_t k, const char *cache_path,
+                          tbfs_options *opt, int32_t *from_cache);
+
 /* Betweenness centrality over the given roots: bc[v] = sum over roots s != v
  * of Brandes' dependency delta_s(v) (U. Brandes, J. Math. Sociology 25(2),
  * 2001), unnormalised; on an undirected graph every pair is counted in both

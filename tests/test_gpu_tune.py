@@ -1,0 +1,50 @@
+"""Degree profile on the device against the host restatement, and the
+autotuner: candidates, cache round trip, results unchanged under tuned
+parameters."""
+import numpy as np
+import pytest
+
+import turbobfs_gb300 as tb
+from turbobfs_gb300 import graphs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("kind", ["rmat", "grid", "directed"])
+def test_device_degree_profile_matches_host(gpu_available, kind):
+    if kind == "rmat":
+        h = graphs.rmat(14, 16, seed=1)
+    elif kind == "grid":
+        h = graphs.grid(100, seed=1)
+    else:
+        rng = np.random.default_rng(2)
+        h = graphs.from_edges(5000, rng.integers(0, 5000, 30000, dtype=np.int32),
+                              rng.integers(0, 5000, 30000, dtype=np.int32))
+    want = graphs.degree_profile(h)
+    with tb.Graph.from_host_csc(h) as g:
+        got = g.degree_profile()
+    assert np.array_equal(got["hist"], np.asarray(want["hist_log2"], dtype=np.int64))
+    assert got["max"] == want["max"]
+    assert abs(got["mean"] - want["mean"]) < 1e-12
+
+
+def test_autotune_candidates_cache_and_results(gpu_available, tmp_path):
+    h = graphs.rmat(15, 16, seed=3)
+    roots = graphs.pick_roots(h, 3, seed=3)
+    cache = str(tmp_path / "tune.txt")
+    with tb.Graph.from_host_csc(h) as g:
+        t1 = g.autotune(roots, cache=cache)
+        assert not t1["from_cache"]
+        assert t1["alpha"] in (2.0, 5.0, 15.0, 40.0, 120.0)
+        assert t1["beta"] in (2.0, 6.0, 18.0, 54.0, 162.0)
+        assert t1["pull_ratio"] in (0.25, 1.0, 4.0, 16.0)
+        t2 = g.autotune(roots, cache=cache)
+        assert t2["from_cache"] and (t2["alpha"], t2["beta"], t2["pull_ratio"]) == \
+            (t1["alpha"], t1["beta"], t1["pull_ratio"])
+        # the same family and scale shares the key
+        with tb.Graph.from_host_csc(graphs.rmat(15, 16, seed=4)) as g2:
+            assert g2.autotune(graphs.pick_roots(h, 1, seed=1), cache=cache)["from_cache"]
+        base = g.bfs(int(roots[0]))
+        tuned = g.bfs(int(roots[0]), alpha=t1["alpha"], beta=t1["beta"],
+                      pull_ratio=t1["pull_ratio"])
+        assert np.array_equal(base.S, tuned.S) and np.array_equal(base.sigma, tuned.sigma)

@@ -91,6 +91,9 @@ _SIGNATURES = {
                               POINTER(Stats)]),
     "tbfs_bfs_batch": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_int32, c_void_p,
                                c_void_p, POINTER(Stats)]),
+    "tbfs_graph_degree_profile": (c_int, [c_void_p, _P_I64, _P_I64, POINTER(c_double)]),
+    "tbfs_autotune": (c_int, [c_void_p, _P_I32, c_int32, c_char_p, POINTER(Options),
+                              POINTER(c_int32)]),
     "tbfs_brandes": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_void_p,
                              POINTER(c_int32)]),
     "tbfs_arena_create": (c_int, [c_int32, _P_I32, _P_I64, _P_I32, _P_I32, c_uint32,

@@ -184,6 +184,28 @@ class Graph:
             out[0]["trace"], out[0]["trace_end_us"] = _parse_trace(tr)
         return S, sg, out
 
+    def degree_profile(self) -> dict:
+        """{'hist': int64[40] (vertices per floor(log2(deg+1))), 'max', 'mean'},
+        computed on the device."""
+        h = np.zeros(40, dtype=np.int64)
+        mx = ctypes.c_int64()
+        mean = ctypes.c_double()
+        check(lib().tbfs_graph_degree_profile(self.handle, _ptr(h, _P_I64), ctypes.byref(mx),
+                                              ctypes.byref(mean)), "tbfs_graph_degree_profile")
+        return {"hist": h, "max": int(mx.value), "mean": float(mean.value)}
+
+    def autotune(self, roots, cache: str | None = None, **kw) -> dict:
+        """Tuned {'alpha', 'beta', 'pull_ratio', 'from_cache'} for this graph
+        (timed on ``roots``; cached per degree profile in ``cache``)."""
+        roots = _i32(roots)
+        o = make_options("auto", True, **kw)
+        fc = ctypes.c_int32()
+        check(lib().tbfs_autotune(self.handle, _ptr(roots, _P_I32), int(roots.shape[0]),
+                                  cache.encode() if cache else None, ctypes.byref(o),
+                                  ctypes.byref(fc)), "tbfs_autotune")
+        return {"alpha": o.alpha, "beta": o.beta, "pull_ratio": o.pull_ratio,
+                "from_cache": bool(fc.value)}
+
     def betweenness(self, roots=None, **kw):
         """Brandes betweenness over ``roots`` (default: every vertex):
         (bc float64[n], number of roots whose path counts overflowed).
