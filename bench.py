@@ -57,6 +57,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--cpu-threads", type=int, default=0)
+    p.add_argument("--no-autotune", action="store_true",
+                   help="default alpha/beta/pull_ratio instead of the autotuned ones")
     p.add_argument("--part", choices=["all", "batched", "serving"], default="all",
                    help="batched / serving: run only that report and print it (profiling)")
     p.add_argument("--no-batched", action="store_true", help="skip the batched report")
@@ -271,7 +273,14 @@ def run_tbfs(args, world, rank, local):
     g = tb.Graph.from_host_csc(h)
     S_dev = torch.empty((k, n), dtype=torch.int32, device="cuda")
     sg_dev = torch.empty((k, n), dtype=torch.int64, device="cuda")
-    o = make_options(args.mode, True, outputs_on_device=True)
+    tuning = {"autotuned": False}
+    kw = {}
+    if not args.no_autotune and args.mode == "auto":
+        # the library's autotuner, timed on 4 of the roots (not cached)
+        tu = g.autotune(roots[:4])
+        kw = {"alpha": tu["alpha"], "beta": tu["beta"], "pull_ratio": tu["pull_ratio"]}
+        tuning = {"autotuned": True, "sample_roots": 4, **kw}
+    o = make_options(args.mode, True, outputs_on_device=True, **kw)
     stats = (_lib.Stats * k)()
     roots_c = np.ascontiguousarray(roots, dtype=np.int32)
     import ctypes
@@ -332,7 +341,8 @@ def run_tbfs(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "int64",
         "data": "synthetic (seeded RMAT generator; no public dataset named)",
         "impl": "tbfs",
-        "config": config(h, k, world, {"mode": args.mode, "outputs": "S int32 + sigma int64 in HBM",
+        "config": config(h, k, world, {"mode": args.mode, "tuning": tuning,
+                                       "outputs": "S int32 + sigma int64 in HBM",
                                        "levels_min_max": [min(levels), max(levels)],
                                        "td_bu_levels_root0": [per_root[0]["td_levels"],
                                                               per_root[0]["bu_levels"]]}),
@@ -389,6 +399,7 @@ def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
         ic[:] = h.row_idx
         o = make_options("auto", True)
         o.alpha, o.beta, o.mode = o_dev.alpha, o_dev.beta, o_dev.mode
+        o.pull_ratio = o_dev.pull_ratio
         stats = (_lib.Stats * k)()
 
         def one():

@@ -75,7 +75,7 @@ namespace {
 
 using dev::FULL;
 using dev::add_chk;
-using dev::smem_add64;
+using dev::smem_add_split;
 using dev::global_ns;
 using dev::grid_barrier;
 using dev::warp_find_owner;
@@ -94,7 +94,10 @@ enum SigMode {
 };
 
 struct WarpWin {
-  unsigned long long val[kWin]; /* PULL: accumulator; PUSH: entry's sigma   */
+  /* PULL: accumulator of the entry; PUSH: the entry's sigma -- as low and
+   * high words in separate arrays, so that neighbouring entries fall in
+   * different banks */
+  unsigned lo[kWin], hi[kWin];
   int v[kWin];                  /* vertex of the entry                      */
   int a[kWin];                  /* list index of its first window edge      */
   unsigned s[kWin + 1];         /* window-relative start of its edges       */
@@ -190,8 +193,15 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
       w.v[k] = v;
       w.a[k] = __ldcg(Q.a + i) + (int)(b - eb);
       w.s[k] = bc - pos;
-      if (SIG == SIG_PULL) w.val[k] = 0ull;
-      if (SIG == SIG_PUSH_NEW || SIG == SIG_PUSH_AT) w.val[k] = p.sigma[v];
+      if (SIG == SIG_PULL) {
+        w.lo[k] = 0u;
+        w.hi[k] = 0u;
+      }
+      if (SIG == SIG_PUSH_NEW || SIG == SIG_PUSH_AT) {
+        const unsigned long long x = p.sigma[v];
+        w.lo[k] = (unsigned)x;
+        w.hi[k] = (unsigned)(x >> 32);
+      }
     }
     if (lane == 0) {
       const unsigned ee = (i0 + nw < Q.qn) ? (unsigned)__ldcg(Q.e + i0 + nw) : Q.qe;
@@ -285,7 +295,8 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
         for (int j = 0; j < kEPT; ++j) {
           const bool add = SIG == SIG_PUSH_NEW ? ((hit >> j) & 1u) != 0 : ((in >> j) & 1u) != 0;
           if (add) {
-            const unsigned long long x = w.val[kk[j]];
+            const unsigned long long x =
+                ((unsigned long long)w.hi[kk[j]] << 32) | (unsigned long long)w.lo[kk[j]];
             add_chk(atomicAdd(p.sigma + u[j], x), x, ovf);
           }
         }
@@ -299,19 +310,19 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
 #pragma unroll
         for (int j = 0; j < kEPT; ++j) {
           if (kk[j] != rk) {
-            if (run) smem_add64(&w.val[rk], run, ovf);
+            if (run) smem_add_split(&w.lo[rk], &w.hi[rk], run, ovf);
             rk = kk[j];
             run = 0;
           }
           run = add_chk(run, c[j], ovf);
         }
-        if (run) smem_add64(&w.val[rk], run, ovf);
+        if (run) smem_add_split(&w.lo[rk], &w.hi[rk], run, ovf);
       }
     }
     __syncwarp();
     if (SIG == SIG_PULL) {
       for (unsigned k = lane; k < nw; k += 32) {
-        const unsigned long long x = w.val[k];
+        const unsigned long long x = ((unsigned long long)w.hi[k] << 32) | (unsigned long long)w.lo[k];
         if (x) add_chk(atomicAdd(p.sigma + w.v[k], x), x, ovf);
       }
     }

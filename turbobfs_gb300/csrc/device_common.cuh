@@ -1,6 +1,6 @@
 /*
  * device_common.cuh -- device helpers shared by the persistent traversal
- * kernels (single-source engine and frontier-matrix batch engine).
+ * kernels (single-source, frontier-matrix batch, multi-instance, Brandes).
  */
 #ifndef TBFS_DEVICE_COMMON_CUH
 #define TBFS_DEVICE_COMMON_CUH
@@ -42,18 +42,18 @@ __device__ __forceinline__ unsigned long long add_chk(unsigned long long a,
   return s;
 }
 
-/* *acc += x for a 64-bit accumulator in shared memory, with two native
- * 32-bit atomics: the low word's returned old value yields the carry, which
- * is folded into the high word's add; the high word's returned old value
- * detects sums reaching 2^63.  Exact modulo 2^64 under any interleaving. */
-__device__ __forceinline__ void smem_add64(unsigned long long *acc, unsigned long long x,
-                                           bool &ovf) {
-  unsigned *w = reinterpret_cast<unsigned *>(acc);
+/* *acc += x for a 64-bit accumulator in shared memory kept as two words in
+ * separate arrays (*lo, *hi), with two native 32-bit atomics: the low word's
+ * returned old value yields the carry, which is folded into the high word's
+ * add; the high word's returned old value detects sums reaching 2^63.
+ * Exact modulo 2^64 under any interleaving. */
+__device__ __forceinline__ void smem_add_split(unsigned *lo, unsigned *hi, unsigned long long x,
+                                               bool &ovf) {
   const unsigned xl = (unsigned)x, xh = (unsigned)(x >> 32);
-  const unsigned old_l = atomicAdd(w, xl);
+  const unsigned old_l = atomicAdd(lo, xl);
   const unsigned carry = (old_l + xl) < old_l ? 1u : 0u;
   const unsigned add_h = xh + carry;
-  const unsigned old_h = atomicAdd(w + 1, add_h);
+  const unsigned old_h = atomicAdd(hi, add_h);
   const unsigned new_h = old_h + add_h;
   if (new_h < old_h || (new_h >> 31) || add_h < xh) ovf = true;
 }
