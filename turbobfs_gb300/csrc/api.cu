@@ -115,6 +115,9 @@ static void graph_free(tbfs_graph *g) {
   cudaFree(g->ctl);
   cudaFree(g->S_dev);
   cudaFree(g->sigma_dev);
+  cudaFree(g->S_dev2);
+  cudaFree(g->sigma_dev2);
+  if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
   cudaFree(g->trace_dev);
   if (g->ctl_host) cudaFreeHost(g->ctl_host);
   if (g->ev0) cudaEventDestroy(g->ev0);
@@ -518,29 +521,57 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
   }
   CUDA_TRY(cudaSetDevice(g->device));
   cudaStream_t s = (cudaStream_t)o.stream;
+  const bool host_out = !o.outputs_on_device;
+  const bool want_sigma = o.want_sigma != 0;
   tbfs_status st = TBFS_OK;
-  if (!o.outputs_on_device && (st = ensure_result_buffers(g, o.want_sigma != 0)) != TBFS_OK)
-    return st;
+  /* host outputs: two device result buffers; the copies of root i run on
+   * the copy stream while root i+1 is traversed on s */
+  if (host_out) {
+    if ((st = ensure_result_buffers(g, want_sigma)) != TBFS_OK) return st;
+    if (!g->S_dev2) CUDA_TRY(cudaMalloc(&g->S_dev2, (size_t)g->n * sizeof(int)));
+    if (want_sigma && !g->sigma_dev2)
+      CUDA_TRY(cudaMalloc(&g->sigma_dev2, (size_t)g->n * sizeof(unsigned long long)));
+    if (!g->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+  }
   std::vector<cudaEvent_t> ev(2 * (size_t)k, nullptr);
+  std::vector<cudaEvent_t> ready((size_t)k, nullptr), copied((size_t)k, nullptr);
   BfsCtl *ctl_h = nullptr;
   cudaError_t e = cudaMallocHost(&ctl_h, (size_t)k * sizeof(BfsCtl));
   for (size_t i = 0; e == cudaSuccess && i < ev.size(); ++i) e = cudaEventCreate(&ev[i]);
+  for (int32_t i = 0; host_out && e == cudaSuccess && i < k; ++i) {
+    e = cudaEventCreateWithFlags(&ready[(size_t)i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied[(size_t)i], cudaEventDisableTiming);
+  }
   const size_t n = (size_t)g->n;
   for (int32_t i = 0; e == cudaSuccess && st == TBFS_OK && i < k; ++i) {
-    int *S_dst = o.outputs_on_device ? S + i * n : g->S_dev;
-    unsigned long long *sig_dst =
-        o.outputs_on_device ? reinterpret_cast<unsigned long long *>(sigma) + (o.want_sigma ? i * n : 0)
-                            : g->sigma_dev;
+    int *S_dst;
+    unsigned long long *sig_dst;
+    if (host_out) {
+      S_dst = (i & 1) ? g->S_dev2 : g->S_dev;
+      sig_dst = (i & 1) ? g->sigma_dev2 : g->sigma_dev;
+      /* the buffer's previous results must be on their way home first */
+      if (i >= 2) e = cudaStreamWaitEvent(s, copied[(size_t)i - 2], 0);
+      if (e != cudaSuccess) break;
+    } else {
+      S_dst = S + i * n;
+      sig_dst = reinterpret_cast<unsigned long long *>(sigma) + (want_sigma ? i * n : 0);
+    }
     const BfsParams p = make_params(g, roots[i], o, S_dst, sig_dst);
     st = enqueue_bfs(g, p, s, ev[2 * i], ev[2 * i + 1], ctl_h + i);
-    if (st == TBFS_OK && !o.outputs_on_device) {
-      e = cudaMemcpyAsync(S + i * n, S_dst, n * sizeof(int), cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess && o.want_sigma)
-        e = cudaMemcpyAsync(sigma + i * n, sig_dst, n * sizeof(int64_t),
-                            cudaMemcpyDeviceToHost, s);
+    if (st == TBFS_OK && host_out) {
+      e = cudaEventRecord(ready[(size_t)i], s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(g->copy_stream, ready[(size_t)i], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(S + i * n, S_dst, n * sizeof(int), cudaMemcpyDeviceToHost,
+                            g->copy_stream);
+      if (e == cudaSuccess && want_sigma)
+        e = cudaMemcpyAsync(sigma + i * n, sig_dst, n * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                            g->copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(copied[(size_t)i], g->copy_stream);
     }
   }
   if (e == cudaSuccess && st == TBFS_OK) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && st == TBFS_OK && host_out) e = cudaStreamSynchronize(g->copy_stream);
   for (int32_t i = 0; e == cudaSuccess && st == TBFS_OK && i < k; ++i) {
     tbfs_stats tmp = {};
     st = stats_from(ctl_h[i], ev[2 * i], ev[2 * i + 1], &tmp);
@@ -548,7 +579,12 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
     g->last = tmp;
     g->depth_hint = tmp.levels;
   }
+  if (host_out && g->copy_stream) cudaStreamSynchronize(g->copy_stream); /* also on error paths */
   for (auto x : ev)
+    if (x) cudaEventDestroy(x);
+  for (auto x : ready)
+    if (x) cudaEventDestroy(x);
+  for (auto x : copied)
     if (x) cudaEventDestroy(x);
   if (ctl_h) cudaFreeHost(ctl_h);
   g->pending = false;

@@ -283,14 +283,46 @@ __global__ void permuted_degree_kernel(const int *cp, const int *perm, int n, in
 }
 
 /* one warp per new column i copies old column perm[i], renaming its rows */
-__global__ void permuted_lists_kernel(const int *cp, const int *ic, const int *perm,
-                                      const int *inv, const int *cp2, int n, int *ic2) {
+/* New list i is old list perm[i] with every entry renamed by inv, in the same
+ * order.  Short lists (< 32 entries) are copied by one lane each; long ones
+ * are collected into `longs` (count in longs[-1] ... see below) and copied by
+ * a block each, so that a hub's list is spread over 256 threads. */
+__global__ void permuted_short_lists_kernel(const int *cp, const int *ic, const int *perm,
+                                            const int *inv, const int *cp2, int n, int *ic2,
+                                            int *longs, int *nlong) {
   const unsigned lane = threadIdx.x & 31;
-  const unsigned long long w0 = gtid() >> 5, nw = gstride() >> 5;
-  for (unsigned long long i = w0; i < (unsigned long long)n; i += nw) {
+  for (unsigned long long base = gtid() & ~31ull; base < (unsigned long long)n; base += gstride()) {
+    const unsigned long long i = base + lane;
+    int b = 0, len = 0, o = 0;
+    if (i < (unsigned long long)n) {
+      const int v = perm[i];
+      b = cp[v];
+      len = cp[v + 1] - b;
+      o = cp2[i];
+    }
+    if (len < 32)
+      for (int t = 0; t < len; ++t) ic2[o + t] = inv[ic[b + t]];
+    /* append the long ones, one atomic per warp */
+    const bool lng = len >= 32;
+    const unsigned bal = __ballot_sync(0xffffffffu, lng);
+    if (bal) {
+      int pos = 0;
+      if (lane == 0) pos = atomicAdd(nlong, __popc(bal));
+      pos = __shfl_sync(0xffffffffu, pos, 0);
+      if (lng) longs[pos + __popc(bal & ((1u << lane) - 1u))] = (int)i;
+    }
+  }
+}
+
+__global__ void permuted_long_lists_kernel(const int *cp, const int *ic, const int *perm,
+                                           const int *inv, const int *cp2, const int *longs,
+                                           const int *nlong, int *ic2) {
+  const int cnt = *nlong;
+  for (int j = blockIdx.x; j < cnt; j += gridDim.x) {
+    const int i = longs[j];
     const int v = perm[i];
     const int b = cp[v], len = cp[v + 1] - b, o = cp2[i];
-    for (int t = (int)lane; t < len; t += 32) ic2[o + t] = inv[ic[b + t]];
+    for (int t = threadIdx.x; t < len; t += blockDim.x) ic2[o + t] = inv[ic[b + t]];
   }
 }
 
@@ -322,11 +354,18 @@ cudaError_t degree_group_relabel(const int *cp, const int *ic, int n, long long 
       e = cudaGetLastError();
       if (e == cudaSuccess) e = cudaMemsetAsync(cp2 + n, 0, sizeof(int), s);
       if (e == cudaSuccess) e = exclusive_scan(cp2, (long long)n + 1, cp2, s);
+      int *longs = nullptr; /* long lists' new ids, their count after them */
+      if (e == cudaSuccess) e = cudaMalloc(&longs, ((size_t)n + 1) * sizeof(int));
+      if (e == cudaSuccess) e = cudaMemsetAsync(longs + n, 0, sizeof(int), s);
       if (e == cudaSuccess) {
-        permuted_lists_kernel<<<grid_for((long long)n * 32), kThreads, 0, s>>>(cp, ic, perm, inv,
-                                                                               cp2, n, ic2);
+        permuted_short_lists_kernel<<<grid_for(n), kThreads, 0, s>>>(cp, ic, perm, inv, cp2, n,
+                                                                    ic2, longs, longs + n);
+        permuted_long_lists_kernel<<<4096, kThreads, 0, s>>>(cp, ic, perm, inv, cp2, longs,
+                                                             longs + n, ic2);
         e = cudaGetLastError();
       }
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      cudaFree(longs);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     }
   }

@@ -258,6 +258,11 @@ struct tbfs_graph {
   tbfs::BfsCtl *ctl_host = nullptr; /* pinned mirror */
   int *S_dev = nullptr;
   unsigned long long *sigma_dev = nullptr;
+  /* second result buffer and a copy stream: tbfs_bfs_many with host outputs
+   * copies root i's results back while root i+1 is traversed */
+  int *S_dev2 = nullptr;
+  unsigned long long *sigma_dev2 = nullptr;
+  cudaStream_t copy_stream = nullptr;
   long long *trace_dev = nullptr; /* per-level trace records */
   int trace_cap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
