@@ -67,7 +67,7 @@ constexpr int kClear = 256;       /* queue entries per row-clearing item        
 constexpr int kVCost = 4;         /* a vertex costs like this many list entries */
 constexpr long long kItemCost = 1024; /* list entries + vertex costs per item    */
 #ifndef TBFS_BATCH_HITS
-#define TBFS_BATCH_HITS 6
+#define TBFS_BATCH_HITS 3
 #endif
 constexpr int kHitBatch = TBFS_BATCH_HITS; /* hit rows whose counts are fetched per round trip */
 constexpr int kStageU64 = kHitBatch * 32 * 8; /* per-warp stage: hits x lanes x 8 counts */
@@ -628,8 +628,12 @@ __device__ __forceinline__ unsigned upper_owner(const T *pre, unsigned cnt, unsi
 
 /* ---- the kernel ------------------------------------------------------------- */
 
+#ifndef TBFS_BATCH_MINB
+#define TBFS_BATCH_MINB 3 /* 3 CTAs of 256 per SM: 24 warps hide more latency than 128 registers would save */
+#endif
+
 template <int W, bool SIG>
-__global__ void __launch_bounds__(kBlock, 2) fm_bfs_kernel(const BatchParams p) {
+__global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const BatchParams p) {
   constexpr int PER = Grp<W>::PER_WARP;
   constexpr int RS = 32 * W;
   __shared__ __align__(16) unsigned s_m[kWarps][32 * W];
