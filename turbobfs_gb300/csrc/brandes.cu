@@ -43,10 +43,7 @@ constexpr int kWarpDegree = 32;   /* out-degree from which a warp sums a vertex 
 struct __align__(128) SweepCtl {
   int status, timeout_level;
   int pad0[30];
-  unsigned bar_arrive;
-  unsigned pad1[31];
-  unsigned bar_gen;
-  unsigned pad2[31];
+  GridBarrier bar;
 };
 
 struct SweepParams {

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "tbfs.h"
+#include "tbfs_internal.h"
 
 namespace tbfs {
 namespace dev {
@@ -58,10 +59,19 @@ __device__ __forceinline__ void smem_add_split(unsigned *lo, unsigned *hi, unsig
   if (new_h < old_h || (new_h >> 31) || add_h < xh) ovf = true;
 }
 
-/* Grid-wide barrier over a control block with fields bar_arrive, bar_gen
- * (each on its own cache line), status and timeout_level.  Thread 0 of every
- * CTA arrives on the counter; the last one resets it and bumps the
- * generation word.  Every wait is bounded by timeout_ns of wall time
+#ifndef TBFS_BAR_GROUP
+#define TBFS_BAR_GROUP 0
+#endif
+
+/* Grid-wide barrier over a control block with fields bar (GridBarrier),
+ * status and timeout_level.  Thread 0 of every CTA arrives; the last one to
+ * arrive resets the counter and bumps the generation word, on which the
+ * others wait.  With TBFS_BAR_GROUP > 0 the arrivals are two-level: CTAs
+ * arrive on their group's counter (groups of TBFS_BAR_GROUP consecutive
+ * CTAs), and only the last of each group arrives on the top counter, so no
+ * one address takes more than max(group size, groups) arrivals.  Fences
+ * before every arrival carry each CTA's writes along the chain to the
+ * releasing store.  Every wait is bounded by timeout_ns of wall time
  * (globaltimer): on expiry the CTA records TBFS_ERR_TIMEOUT and returns
  * false, and so does every CTA that sees the error word set, so the kernel
  * always terminates.  `level` is recorded (+2) in timeout_level. */
@@ -71,17 +81,31 @@ __device__ bool grid_barrier(Ctl *ctl, long long timeout_ns, int level) {
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned gen = ld_acquire_u32(&ctl->bar_gen);
+    const unsigned gen = ld_acquire_u32(&ctl->bar.gen);
     __threadfence();
-    const unsigned prev = atomicAdd(&ctl->bar_arrive, 1u);
-    if (prev == gridDim.x - 1) {
-      atomicExch(&ctl->bar_arrive, 0u);
+    bool last = false;
+    if (TBFS_BAR_GROUP > 0 && gridDim.x > (unsigned)TBFS_BAR_GROUP) {
+      const unsigned g = blockIdx.x / (unsigned)TBFS_BAR_GROUP;
+      const unsigned groups = (gridDim.x + TBFS_BAR_GROUP - 1) / TBFS_BAR_GROUP;
+      const unsigned gsize =
+          g + 1 < groups ? (unsigned)TBFS_BAR_GROUP : gridDim.x - g * (unsigned)TBFS_BAR_GROUP;
+      unsigned *gc = &ctl->bar.grp[g % tbfs::kBarGroups][0];
+      if (atomicAdd(gc, 1u) == gsize - 1) {
+        atomicExch(gc, 0u);
+        __threadfence();
+        last = atomicAdd(&ctl->bar.arrive, 1u) == groups - 1;
+      }
+    } else {
+      last = atomicAdd(&ctl->bar.arrive, 1u) == gridDim.x - 1;
+    }
+    if (last) {
+      atomicExch(&ctl->bar.arrive, 0u);
       __threadfence();
-      st_release_u32(&ctl->bar_gen, gen + 1);
+      st_release_u32(&ctl->bar.gen, gen + 1);
     } else {
       const unsigned long long t0 = global_ns();
       unsigned spins = 0;
-      while (ld_acquire_u32(&ctl->bar_gen) == gen) {
+      while (ld_acquire_u32(&ctl->bar.gen) == gen) {
         if ((++spins & 31u) == 0) {
           if (ld_volatile(&ctl->status) != 0) {
             ok = 0;

@@ -38,6 +38,10 @@ namespace {
 using dev::FULL;
 using dev::grid_barrier;
 
+#ifndef TBFS_MULTI_PER_SM
+#define TBFS_MULTI_PER_SM 3
+#endif
+
 constexpr int kBlock = 256;
 constexpr int kEPT = 4;                   /* consecutive edges per lane per round */
 constexpr unsigned kRoundEdges = 32 * kEPT;
@@ -356,9 +360,9 @@ cudaError_t multi_geometry(int device, LaunchGeom *out) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, multi_bfs_kernel, kBlock, 0);
   if (e != cudaSuccess) return e;
   if (per < 1) return cudaErrorInvalidConfiguration;
-  /* two CTAs (16 warps) per SM: enough to cover the latency of the pushes,
-   * and half the barrier arrivals of a fully occupied grid */
-  if (per > 2) per = 2;
+  /* a few CTAs per SM: enough warps to cover the latency of the pushes,
+   * fewer barrier arrivals than a fully occupied grid */
+  if (per > TBFS_MULTI_PER_SM) per = TBFS_MULTI_PER_SM;
   out->block = kBlock;
   out->grid = sms * per;
   return cudaSuccess;

@@ -31,11 +31,11 @@
 
 namespace {
 
-constexpr size_t kCtlBytes = 1024; /* control block + validation flag */
+constexpr size_t kCtlBytes = 8192; /* control block + validation flag */
 constexpr size_t kQueueBytes = (size_t)TBFS_NOALLOC_MAX_VERTICES * sizeof(int);
 constexpr size_t kBitmapBytes = (size_t)TBFS_NOALLOC_MAX_VERTICES / 8;
 constexpr size_t kScratchBytes = kCtlBytes + 9 * kQueueBytes + 4 * kBitmapBytes;
-constexpr size_t kFlagOffset = 768;
+constexpr size_t kFlagOffset = kCtlBytes - 256;
 static_assert(sizeof(tbfs::BfsCtl) <= kFlagOffset, "control block must fit its slot");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];

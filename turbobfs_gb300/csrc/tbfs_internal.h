@@ -28,6 +28,18 @@
 
 namespace tbfs {
 
+/* Words of the hand-written grid barrier (device_common.cuh): the top-level
+ * arrival counter and the generation word on their own 128-byte lines, then
+ * one arrival counter per group of CTAs, each on its own line. */
+constexpr int kBarGroups = 32; /* groups of up to TBFS_BAR_GROUP CTAs */
+struct __align__(128) GridBarrier {
+  unsigned arrive;
+  unsigned pad0[31];
+  unsigned gen;
+  unsigned pad1[31];
+  unsigned grp[kBarGroups][32];
+};
+
 /* Device control block of one traversal; zeroed before every launch. */
 struct __align__(128) BfsCtl {
   /* slot d % 3 accumulates the queue of level d+1 ... see bfs_engine.cu */
@@ -39,11 +51,7 @@ struct __align__(128) BfsCtl {
   long long visited, edges;
   unsigned int work[4]; /* dynamic work counter of phase d in work[d % 4] */
   unsigned int pad0[10];
-  /* barrier words on their own 128-byte lines */
-  unsigned int bar_arrive;
-  unsigned int pad1[31];
-  unsigned int bar_gen;
-  unsigned int pad2[31];
+  GridBarrier bar;
 };
 
 struct BfsParams {
@@ -98,10 +106,7 @@ struct __align__(128) BatchCtl {
   int pad0;
   unsigned ovf[8]; /* bit r: a path count of root r reached 2^63 */
   unsigned pad1[2];
-  unsigned bar_arrive;
-  unsigned pad2[31];
-  unsigned bar_gen;
-  unsigned pad3[31];
+  GridBarrier bar;
 };
 
 struct BatchParams {
@@ -193,10 +198,7 @@ struct __align__(128) MultiCtl {
   int phases;                 /* levels run by the launch */
   int stop;                   /* end the launch after the current level */
   int pad0[24];
-  unsigned bar_arrive;
-  unsigned pad1[31];
-  unsigned bar_gen;
-  unsigned pad2[31];
+  GridBarrier bar;
 };
 
 struct MultiParams {
