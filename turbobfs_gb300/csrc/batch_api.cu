@@ -104,7 +104,10 @@ tbfs_status ensure_ws(tbfs_graph *g, int W, bool sigma, cudaStream_t s) {
     TRY(cudaMalloc(&w->F, 3 * n * W * sizeof(unsigned)), "alloc rows");
     TRY(cudaMalloc(&w->S_int, n * rs * sizeof(int)), "alloc depth rows");
     if (keep_sigma) TRY(cudaMalloc(&w->sig_int, n * rs * sizeof(unsigned long long)), "alloc count rows");
-    w->seg_len = 128 * W; /* a hub segment is about one work item of the pull */
+#ifndef TBFS_BATCH_SEG
+#define TBFS_BATCH_SEG 128
+#endif
+    w->seg_len = TBFS_BATCH_SEG * W; /* a hub segment: about one work item of the pull */
     TRY(batch_hubs(g->cp, g->n, w->seg_len, &w->hubs, &w->hub_seg, &w->nhub, &w->hub_segs, s),
         "hub list");
     w->W = W;

@@ -35,9 +35,11 @@
  *         counts over the in-lists of the new queue only.
  *
  * Direction rule per level: push while the frontier queue's out-edges times
- * alpha are below the in-list entries of vertices not yet reached by every
- * root (Beamer, Asanovic, Patterson, SC 2012, with the batch's unexplored
- * edges).
+ * alpha are below what a pull level costs -- the in-list entries of vertices
+ * not yet reached by every root plus kVCost per vertex, since a pull visits
+ * every vertex's seen row (Beamer, Asanovic, Patterson, SC 2012, with the
+ * batch's unexplored edges).  Without the vertex term a pull would follow a
+ * tail level of a few thousand vertices, at the cost of a pass over n.
  *
  * Path counts are exact in uint64; a sum reaching 2^63 sets the root's bit
  * in ctl->ovf.  The fast path ORs the high words of the running sums; only
@@ -65,7 +67,10 @@ constexpr int kWarps = kBlock / 32;
 constexpr int kPushRounds = 8;    /* 32-edge rounds per push work item         */
 constexpr int kClear = 256;       /* queue entries per row-clearing item        */
 constexpr int kVCost = 4;         /* a vertex costs like this many list entries */
-constexpr long long kItemCost = 1024; /* list entries + vertex costs per item    */
+#ifndef TBFS_BATCH_ITEM
+#define TBFS_BATCH_ITEM 512
+#endif
+constexpr long long kItemCost = TBFS_BATCH_ITEM; /* list entries + vertex costs per item */
 #ifndef TBFS_BATCH_HITS
 #define TBFS_BATCH_HITS 3
 #endif
@@ -183,6 +188,24 @@ __device__ __forceinline__ void group_or(unsigned (&x)[W], unsigned gmask) {
     for (int w = 0; w < W; ++w) x[w] |= __shfl_xor_sync(gmask, x[w], o);
 }
 
+/* found as left by scan_list -> the group's found row in every lane */
+template <int W, bool SIG>
+__device__ __forceinline__ void finish_found(unsigned (&found)[W], const Grp<W> &g) {
+  if constexpr (SIG) {
+    /* word w holds the bytes of lanes 4w .. 4w+3 */
+    const unsigned b = found[0];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      unsigned x = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) x |= __shfl_sync(g.gmask, b, g.gbase + 4 * w + k) << (8 * k);
+      found[w] = x;
+    }
+  } else {
+    group_or<W>(found, g.gmask);
+  }
+}
+
 /* Per-warp shared memory: m (32 x W words) stages the hit rows' masks;
  * stage (kHitBatch x 4 x 32 lanes x 2 counts) receives the 16-byte chunks of
  * path counts each lane fetches asynchronously for its own roots: chunk q of
@@ -192,13 +215,26 @@ struct WarpSmem {
   unsigned long long *stage;
 };
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-#if TBFS_BATCH_CA
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-#else /* L2 only: the rows are gathered once per hit, L1 reuse is rare */
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-#endif
+/* cp.async of 16 bytes from g + GOFF to shared address s + SOFF when pred is
+ * nonzero: predicated, offsets as immediates */
+template <int SOFF, int GOFF>
+__device__ __forceinline__ void cp_async16_off(unsigned s, const void *g, unsigned pred) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t"
+      "@p cp.async.cg.shared.global [%0+%3], [%1+%4], 16;\n\t}" ::"r"(s),
+      "l"(g), "r"(pred), "n"(SOFF), "n"(GOFF)
+      : "memory");
+}
+
+/* the four root-pair chunks of one hit row for a lane of a G-lane group:
+ * chunk q from g + 16 G q bytes into shared s + 512 q bytes, if pair q of
+ * the lane's byte lm is set */
+template <int G>
+__device__ __forceinline__ void fetch_pairs(unsigned s, const unsigned long long *g, unsigned lm) {
+  cp_async16_off<0, 0>(s, g, lm & 0x03u);
+  cp_async16_off<512, 16 * G>(s, g, lm & 0x0cu);
+  cp_async16_off<1024, 32 * G>(s, g, lm & 0x30u);
+  cp_async16_off<1536, 48 * G>(s, g, lm & 0xc0u);
 }
 
 /* wait for this thread's outstanding cp.async copies */
@@ -228,12 +264,25 @@ template <bool EXACT>
 __device__ __forceinline__ void acc_staged(const unsigned long long *slot, unsigned lm,
                                            unsigned long long (&acc)[8], unsigned &ovh,
                                            unsigned &ovm) {
+  if constexpr (!EXACT) {
+    /* branch-free: every chunk slot is read (a slot not copied this time
+     * holds a stale value, which no add takes), the adds are predicated on
+     * the root bits, and one OR per pair collects both high words */
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    if ((lm >> (2 * q)) & 3u) {
+    for (int q = 0; q < 4; ++q) {
       const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(slot + q * 64);
-      add1<EXACT>(acc[2 * q], x.x, lm, 2 * q, ovh, ovm);
-      add1<EXACT>(acc[2 * q + 1], x.y, lm, 2 * q + 1, ovh, ovm);
+      if (lm & (1u << (2 * q))) acc[2 * q] += x.x;
+      if (lm & (2u << (2 * q))) acc[2 * q + 1] += x.y;
+      ovh |= (unsigned)(acc[2 * q] >> 32) | (unsigned)(acc[2 * q + 1] >> 32);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if ((lm >> (2 * q)) & 3u) {
+        const ulonglong2 x = *reinterpret_cast<const ulonglong2 *>(slot + q * 64);
+        add1<EXACT>(acc[2 * q], x.x, lm, 2 * q, ovh, ovm);
+        add1<EXACT>(acc[2 * q + 1], x.y, lm, 2 * q + 1, ovh, ovm);
+      }
     }
   }
 }
@@ -249,9 +298,13 @@ __device__ __forceinline__ void report_overflow(const BatchParams &p, unsigned o
   }
 }
 
-/* Scan in-list entries [lo, hi) of one vertex with its group.  found |= F_d[u]
- * & want over the entries; with SIG, every lane adds to acc the path counts
- * of its roots set in F_d[u] & want.  sm: the warp's 32 x W staging words. */
+/* Scan in-list entries [lo, hi) of one vertex with its group: the OR of
+ * F_d[u] & want over the entries is collected in found -- without SIG as
+ * rows (each lane its own entries; finish_found ORs them over the group),
+ * with SIG as the lane's own byte in found[0] (finish_found assembles the
+ * row), which keeps seven registers free for the path counts.  With SIG,
+ * every lane also adds to acc the path counts of its roots set in F_d[u] &
+ * want.  sm: the warp's 32 x W staging words. */
 template <int W, bool SIG, bool EXACT>
 __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *Fd, int lo, int hi,
                                           const unsigned (&want)[W], unsigned (&found)[W],
@@ -277,8 +330,10 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
 #pragma unroll
       for (int w = 0; w < W; ++w) m[w] = 0u;
     }
+    if constexpr (!SIG) {
 #pragma unroll
-    for (int w = 0; w < W; ++w) found[w] |= m[w];
+      for (int w = 0; w < W; ++w) found[w] |= m[w];
+    }
     if (SIG) {
       unsigned hits = __ballot_sync(g.gmask, any);
       if (hits) {
@@ -289,6 +344,7 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
          * its roots that are set (16 bytes per root pair) into its own stage
          * slots, waits for its own copies only, then accumulates */
         unsigned long long *mine = sm.stage + g.lane * 2;
+        const unsigned s_mine = (unsigned)__cvta_generic_to_shared(mine);
         do {
           unsigned lms[kHitBatch];
 #pragma unroll
@@ -300,11 +356,9 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
               const int uj = __shfl_sync(g.gmask, u, g.gbase + j);
               const unsigned lm = lane_bits_smem<W>(sm.m + (g.gbase + j) * W, g);
               lms[b] = lm;
+              found[0] |= lm;
               const unsigned long long *row = p.sig_int + (size_t)uj * RS;
-#pragma unroll
-              for (int q = 0; q < 4; ++q)
-                if ((lm >> (2 * q)) & 3u)
-                  cp_async16(mine + (4 * b + q) * 64, row + 2 * (g.gl + G * q));
+              fetch_pairs<G>(s_mine + 2048u * (unsigned)b, row + 2 * g.gl, lm);
             }
           }
           cp_async_wait_all();
@@ -389,21 +443,26 @@ __device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, 
   take = false;
   full = false;
   if (!__any_sync(g.gmask, anyf)) return;
-  group_or<W>(found, g.gmask);
+  finish_found<W, SIG>(found, g);
   if (SIG && __any_sync(g.gmask, (ovh >> 31) != 0u)) {
     ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
     report_overflow<W>(p, ovm, g);
   }
   write_new<W, SIG>(p, d, v, lane_bits<W>(found, g), acc, g);
+  /* seen rows hold valid roots only, so sn = valid & ~want: sn need not
+   * stay live across the scan */
   if (g.gl < W) {
     const unsigned fw = pick<W>(found, g.gl);
     if (fw) {
       F1[(size_t)v * W + g.gl] = fw;
-      p.seen[(size_t)v * W + g.gl] = pick<W>(sn, g.gl) | fw;
+      p.seen[(size_t)v * W + g.gl] = (p.valid[g.gl] & ~pick<W>(want, g.gl)) | fw;
     }
   }
   take = true;
-  full = row_full<W>(p, sn, found);
+  bool f = true;
+#pragma unroll
+  for (int w = 0; w < W; ++w) f &= found[w] == want[w];
+  full = f;
 }
 
 /* Fold a segment's partial result into hub h: new bits into F1 (pull only),
@@ -473,7 +532,7 @@ __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h,
 #pragma unroll
   for (int w = 0; w < W; ++w) anyf |= found[w] != 0u;
   if (__any_sync(g.gmask, anyf)) {
-    group_or<W>(found, g.gmask);
+    finish_found<W, SIG>(found, g);
     commit_segment<W, SIG, true>(p, h, found, acc, ovh, Fd, lo, hi, want, F1, sm, g);
   }
   take = false;
@@ -489,10 +548,13 @@ __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h,
   write_new<W, false>(p, d, h, lane_bits<W>(nx, g), none, g);
   if (g.gl < W) {
     const unsigned fw = pick<W>(nx, g.gl);
-    if (fw) p.seen[(size_t)h * W + g.gl] = pick<W>(sn, g.gl) | fw;
+    if (fw) p.seen[(size_t)h * W + g.gl] = (p.valid[g.gl] & ~pick<W>(want, g.gl)) | fw;
   }
   take = true;
-  full = row_full<W>(p, sn, nx);
+  bool f = true;
+#pragma unroll
+  for (int w = 0; w < W; ++w) f &= nx[w] == want[w];
+  full = f;
 }
 
 /* push level, second phase: counts of the roots new at v (all of them known
@@ -541,7 +603,7 @@ __device__ __forceinline__ void count_segment(const BatchParams &p, int d, int h
 #pragma unroll
   for (int w = 0; w < W; ++w) anyf |= found[w] != 0u;
   if (__any_sync(g.gmask, anyf)) {
-    group_or<W>(found, g.gmask);
+    finish_found<W, true>(found, g);
     commit_segment<W, true, false>(p, h, found, acc, ovh, Fd, lo, hi, want, F1, sm, g);
   }
   full = false;
@@ -659,9 +721,10 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
   }
   for (long long i = tid; i < ((long long)n + 31) / 32; i += nth) p.touched[i] = 0u;
   for (long long i = tid; i < n; i += nth) p.seg_arrive[i] = 0u;
-  if (SIG)
+  if (SIG) {
     for (long long i = tid; i < (long long)p.nhub * RS; i += nth)
       p.sig_int[(size_t)__ldg(p.hubs + i / RS) * RS + i % RS] = 0ull;
+  }
   if (!grid_barrier(ctl, p.timeout_ns, -1)) return;
 
   /* roots (k <= 256 = kBlock): CTA 0 sets their bits, depth 0, count 1, and
@@ -753,7 +816,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
     else if (p.mode == TBFS_MODE_BOTTOM_UP)
       push = false;
     else
-      push = (double)qe * (double)p.alpha < (double)m_unseen;
+      push = (double)qe * (double)p.alpha < (double)m_unseen + (double)kVCost * (double)n;
     if (tid == 0 && p.trace && d < p.trace_cap - 1) {
       long long *rec = p.trace + 4 * (long long)d;
       rec[0] = (long long)dev::global_ns();

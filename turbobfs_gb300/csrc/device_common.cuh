@@ -84,11 +84,11 @@ __device__ bool grid_barrier(Ctl *ctl, long long timeout_ns, int level) {
     const unsigned gen = ld_acquire_u32(&ctl->bar.gen);
     __threadfence();
     bool last = false;
-    if (TBFS_BAR_GROUP > 0 && gridDim.x > (unsigned)TBFS_BAR_GROUP) {
-      const unsigned g = blockIdx.x / (unsigned)TBFS_BAR_GROUP;
-      const unsigned groups = (gridDim.x + TBFS_BAR_GROUP - 1) / TBFS_BAR_GROUP;
-      const unsigned gsize =
-          g + 1 < groups ? (unsigned)TBFS_BAR_GROUP : gridDim.x - g * (unsigned)TBFS_BAR_GROUP;
+    constexpr unsigned kGrp = TBFS_BAR_GROUP > 0 ? (unsigned)TBFS_BAR_GROUP : 1u;
+    if (TBFS_BAR_GROUP > 0 && gridDim.x > kGrp) {
+      const unsigned g = blockIdx.x / kGrp;
+      const unsigned groups = (gridDim.x + kGrp - 1) / kGrp;
+      const unsigned gsize = g + 1 < groups ? kGrp : gridDim.x - g * kGrp;
       unsigned *gc = &ctl->bar.grp[g % tbfs::kBarGroups][0];
       if (atomicAdd(gc, 1u) == gsize - 1) {
         atomicExch(gc, 0u);
