@@ -177,7 +177,7 @@ __device__ __forceinline__ unsigned lane_bits(const unsigned (&row)[W], const Gr
 /* the same for a row in shared memory */
 template <int W>
 __device__ __forceinline__ unsigned lane_bits_smem(const unsigned *row, const Grp<W> &g) {
-  return (row[g.gl >> 2] >> (8 * (g.gl & 3))) & 0xffu;
+  return reinterpret_cast<const unsigned char *>(row)[g.gl]; /* byte gl: words are little-endian */
 }
 
 template <int W>
