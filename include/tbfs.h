@@ -109,6 +109,39 @@ tbfs_status tbfs_graph_create_cooc(const int32_t *row, const int32_t *col,
                                    int32_t n, int64_t nnz, uint32_t flags,
                                    tbfs_graph **out);
 
+/* Build a graph on the device from an edge list: edge k is src[k] ->
+ * dst[k] (0-based), landing in column dst[k].  build_flags are those of the
+ * host builder tbfs_csc_from_edges (tbfs_graphgen.h: TBFS_BUILD_SYMMETRIZE,
+ * _DROP_LOOPS, _DEDUP, _SORT) and give the same col_ptr / row_idx: without
+ * SORT or DEDUP a column keeps the input order of its entries.  Replaces
+ * the reference's host builders CP_RP_ug / SSCCSC_uw / SSCCOOC_uw
+ * (TurboBFS_CSC_TD/sparseformatransf.c:60-104,
+ * TurboBFS_COOC_TD/sparseformatransf.c:62-95) for large graphs.
+ * graph_flags as for tbfs_graph_create_csc (TBFS_GRAPH_SYMMETRIC is implied
+ * by SYMMETRIZE; TBFS_GRAPH_DEVICE_PTRS: src/dst are device pointers). */
+tbfs_status tbfs_graph_create_edges(const int32_t *src, const int32_t *dst, int32_t n,
+                                    int64_t m, uint32_t build_flags, uint32_t graph_flags,
+                                    tbfs_graph **out);
+
+/* Parse Matrix Market coordinate text (a .mtx file's bytes in host memory)
+ * on the device and build the graph from it: entry line k "i j [...]" is
+ * the edge i-1 -> j-1; undirected adds each entry's mirror (a diagonal entry
+ * twice), as the reference's readMMfile_uw + CP_RP_ug
+ * (TurboBFS_CSC_TD/readMMfilef.c:56-70) and the host reader tbfs_mm_read do.
+ * Errors (TBFS_ERR_IO): no banner, not coordinate, no size line, fewer
+ * entry lines than the size line's nz, an index out of range. */
+tbfs_status tbfs_graph_create_mm(const char *text, int64_t bytes, int32_t undirected,
+                                 uint32_t build_flags, uint32_t graph_flags, tbfs_graph **out);
+
+/* tbfs_graph_create_mm on the contents of a file (read into pinned memory). */
+tbfs_status tbfs_graph_load_mm(const char *path, int32_t undirected, uint32_t build_flags,
+                               uint32_t graph_flags, tbfs_graph **out);
+
+/* Copy the resident in-lists (col_ptr[n+1], row_idx[nnz]) to the host.
+ * TBFS_ERR_UNSUPPORTED for a graph stored regrouped by degree (create it
+ * with TBFS_GRAPH_KEEP_ORDER to read it back). */
+tbfs_status tbfs_graph_get_csc(const tbfs_graph *g, int32_t *col_ptr, int32_t *row_idx);
+
 void tbfs_graph_destroy(tbfs_graph *g);
 
 tbfs_status tbfs_graph_info(const tbfs_graph *g, int32_t *n, int64_t *nnz,

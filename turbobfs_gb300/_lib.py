@@ -92,6 +92,12 @@ _SIGNATURES = {
     "tbfs_bfs_batch": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_int32, c_void_p,
                                c_void_p, POINTER(Stats)]),
     "tbfs_graph_degree_profile": (c_int, [c_void_p, _P_I64, _P_I64, POINTER(c_double)]),
+    "tbfs_graph_create_edges": (c_int, [_P_I32, _P_I32, c_int32, c_int64, c_uint32, c_uint32,
+                                        POINTER(c_void_p)]),
+    "tbfs_graph_create_mm": (c_int, [c_char_p, c_int64, c_int32, c_uint32, c_uint32,
+                                     POINTER(c_void_p)]),
+    "tbfs_graph_load_mm": (c_int, [c_char_p, c_int32, c_uint32, c_uint32, POINTER(c_void_p)]),
+    "tbfs_graph_get_csc": (c_int, [c_void_p, _P_I32, _P_I32]),
     "tbfs_autotune": (c_int, [c_void_p, _P_I32, c_int32, c_char_p, POINTER(Options),
                               POINTER(c_int32)]),
     "tbfs_brandes": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_void_p,

@@ -125,6 +125,58 @@ class Graph:
         self._h = h
         return self
 
+    @classmethod
+    def _adopt(cls, h: ctypes.c_void_p, symmetric: bool) -> "Graph":
+        self = cls.__new__(cls)
+        self._h = h
+        n, nnz = ctypes.c_int32(), ctypes.c_int64()
+        check(lib().tbfs_graph_info(h, ctypes.byref(n), ctypes.byref(nnz), None), "tbfs_graph_info")
+        self.n, self.nnz, self.symmetric = int(n.value), int(nnz.value), bool(symmetric)
+        return self
+
+    @classmethod
+    def from_edges(cls, src, dst, n: int, build_flags: int = 0,
+                   keep_order: bool = False) -> "Graph":
+        """Graph built on the device from the edge list src[k] -> dst[k] with
+        the host builder's construction (``graphs.BUILD_*`` flags; the same
+        CSC as ``graphs.from_edges`` with those flags)."""
+        src, dst = _i32(src), _i32(dst)
+        h = ctypes.c_void_p()
+        check(lib().tbfs_graph_create_edges(_ptr(src, _P_I32), _ptr(dst, _P_I32), int(n),
+                                            int(src.shape[0]), int(build_flags),
+                                            _flags(False, keep_order), ctypes.byref(h)),
+              "tbfs_graph_create_edges")
+        return cls._adopt(h, bool(build_flags & 1))
+
+    @classmethod
+    def from_mm_text(cls, text: bytes, undirected: bool = True, build_flags: int = 0,
+                     keep_order: bool = False) -> "Graph":
+        """Graph from Matrix Market coordinate text, parsed on the device."""
+        h = ctypes.c_void_p()
+        check(lib().tbfs_graph_create_mm(text, len(text), 1 if undirected else 0,
+                                         int(build_flags), _flags(False, keep_order),
+                                         ctypes.byref(h)), "tbfs_graph_create_mm")
+        return cls._adopt(h, undirected)
+
+    @classmethod
+    def load_mm(cls, path, undirected: bool = True, build_flags: int = 0,
+                keep_order: bool = False) -> "Graph":
+        """Graph from a Matrix Market file, parsed on the device."""
+        h = ctypes.c_void_p()
+        check(lib().tbfs_graph_load_mm(str(path).encode(), 1 if undirected else 0,
+                                       int(build_flags), _flags(False, keep_order),
+                                       ctypes.byref(h)), f"tbfs_graph_load_mm({path})")
+        return cls._adopt(h, undirected)
+
+    def csc(self):
+        """The resident in-lists (col_ptr, row_idx) in the caller's numbering
+        (graphs created with keep_order=True)."""
+        cp = np.empty(self.n + 1, np.int32)
+        ic = np.empty(max(self.nnz, 1), np.int32)
+        check(lib().tbfs_graph_get_csc(self.handle, _ptr(cp, _P_I32), _ptr(ic, _P_I32)),
+              "tbfs_graph_get_csc")
+        return cp, ic[: self.nnz]
+
     @property
     def handle(self) -> ctypes.c_void_p:
         if self._h is None:

@@ -13,6 +13,7 @@
 
 #include "tbfs.h"
 #include "tbfs_compat.h"
+#include "tbfs_graphgen.h"
 #include "tbfs_internal.h"
 
 using tbfs::BfsCtl;
@@ -319,6 +320,235 @@ extern "C" tbfs_status tbfs_graph_create_cooc(const int32_t *row, const int32_t 
     return st;
   }
   *out = g;
+  return TBFS_OK;
+}
+
+/* ------------------------------------------- device-built graphs */
+
+/* A graph from an edge list already on the device: CSC built there with the
+ * host builder's construction, then the usual regrouping / out-lists. */
+static tbfs_status graph_from_device_edges(const int *d_src, const int *d_dst, int32_t n,
+                                           int64_t m, uint32_t build_flags, uint32_t graph_flags,
+                                           tbfs_graph **out) {
+  tbfs_graph *g = new tbfs_graph();
+  cudaGetDevice(&g->device);
+  g->n = n;
+  g->flags = graph_flags & ~TBFS_GRAPH_DEVICE_PTRS;
+  if (build_flags & TBFS_BUILD_SYMMETRIZE) g->flags |= TBFS_GRAPH_SYMMETRIC;
+  long long nnz = 0;
+  int bad = 0;
+  cudaError_t e = tbfs::csc_from_edges_device(d_src, d_dst, m, n, build_flags, &g->cp, &g->ic,
+                                              &nnz, &bad, 0);
+  if (e != cudaSuccess) {
+    graph_free(g);
+    if (e == cudaErrorInvalidValue) {
+      tbfs_set_error("edge list: more than INT32_MAX list entries");
+      return TBFS_ERR_UNSUPPORTED;
+    }
+    return cuda_fail(e, "edge list -> CSC on the device", __LINE__);
+  }
+  if (bad) {
+    graph_free(g);
+    return invalid("edge list: endpoint outside [0, n)");
+  }
+  if (nnz > INT32_MAX) {
+    graph_free(g);
+    tbfs_set_error("edge list: %lld CSC entries exceed int32", nnz);
+    return TBFS_ERR_UNSUPPORTED;
+  }
+  g->nnz = nnz;
+  int *d_flag = nullptr;
+  e = cudaMalloc(&d_flag, sizeof(int));
+  if (e != cudaSuccess) {
+    graph_free(g);
+    return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
+  }
+  cudaMemset(d_flag, 0, sizeof(int));
+  tbfs_status st = finish_lists(g, d_flag);
+  cudaFree(d_flag);
+  if (st == TBFS_OK) st = graph_finish(g);
+  if (st != TBFS_OK) {
+    graph_free(g);
+    return st;
+  }
+  *out = g;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_graph_create_edges(const int32_t *src, const int32_t *dst,
+                                               int32_t n, int64_t m, uint32_t build_flags,
+                                               uint32_t graph_flags, tbfs_graph **out) {
+  if (!out) return invalid("tbfs_graph_create_edges: null out pointer");
+  *out = nullptr;
+  if (n < 1 || m < 0 || (m > 0 && (!src || !dst)))
+    return invalid("tbfs_graph_create_edges: need n >= 1, m >= 0, arrays");
+  if (m > ((build_flags & TBFS_BUILD_SYMMETRIZE) ? INT32_MAX / 2 : INT32_MAX)) {
+    tbfs_set_error("tbfs_graph_create_edges: too many edges for int32 lists");
+    return TBFS_ERR_UNSUPPORTED;
+  }
+  tbfs_status st = need_device();
+  if (st != TBFS_OK) return st;
+  if (graph_flags & TBFS_GRAPH_DEVICE_PTRS)
+    return graph_from_device_edges(src, dst, n, m, build_flags, graph_flags, out);
+  int *ds = nullptr, *dd = nullptr;
+  const size_t bytes = (size_t)(m > 0 ? m : 1) * sizeof(int);
+  cudaError_t e = cudaMalloc(&ds, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&dd, bytes);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpy(ds, src, (size_t)m * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && m > 0) e = cudaMemcpy(dd, dst, (size_t)m * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) st = graph_from_device_edges(ds, dd, n, m, build_flags, graph_flags, out);
+  cudaFree(ds);
+  cudaFree(dd);
+  if (e != cudaSuccess) return cuda_fail(e, "edge list upload", __LINE__);
+  return st;
+}
+
+/* The Matrix Market header of text[0, bytes): banner, comments, size line.
+ * *data = offset of the first byte after the size line. */
+static tbfs_status mm_header(const char *text, int64_t bytes, long long *M, long long *N,
+                             long long *nz, int64_t *data) {
+  int64_t p = 0;
+  auto line_end = [&](int64_t q) {
+    while (q < bytes && text[q] != '\n') ++q;
+    return q;
+  };
+  int64_t e = line_end(0);
+  const char banner[] = "%%MatrixMarket";
+  if (e < 14 || memcmp(text, banner, 14) != 0) {
+    tbfs_set_error("Matrix Market text has no banner");
+    return TBFS_ERR_IO;
+  }
+  bool coord = false;
+  for (int64_t q = 0; q + 10 <= e; ++q)
+    if (memcmp(text + q, "coordinate", 10) == 0) coord = true;
+  if (!coord) {
+    tbfs_set_error("Matrix Market text is not a coordinate (sparse) matrix");
+    return TBFS_ERR_IO;
+  }
+  p = e < bytes ? e + 1 : e;
+  while (p < bytes) {
+    e = line_end(p);
+    if (text[p] != '%') {
+      char buf[256];
+      const int64_t len = e - p < 255 ? e - p : 255;
+      memcpy(buf, text + p, (size_t)len);
+      buf[len] = 0;
+      if (sscanf(buf, "%lld %lld %lld", M, N, nz) == 3) {
+        *data = e < bytes ? e + 1 : e;
+        if (*M < 0 || *N < 1 || *nz < 0 || *N > INT32_MAX || *M > INT32_MAX) {
+          tbfs_set_error("Matrix Market size line out of range");
+          return TBFS_ERR_IO;
+        }
+        return TBFS_OK;
+      }
+    }
+    p = e < bytes ? e + 1 : e;
+  }
+  tbfs_set_error("Matrix Market text has no size line");
+  return TBFS_ERR_IO;
+}
+
+extern "C" tbfs_status tbfs_graph_create_mm(const char *text, int64_t bytes, int32_t undirected,
+                                            uint32_t build_flags, uint32_t graph_flags,
+                                            tbfs_graph **out) {
+  if (!out) return invalid("tbfs_graph_create_mm: null out pointer");
+  *out = nullptr;
+  if (!text || bytes < 1) return invalid("tbfs_graph_create_mm: empty text");
+  long long M = 0, N = 0, nz = 0;
+  int64_t data = 0;
+  tbfs_status st = mm_header(text, bytes, &M, &N, &nz, &data);
+  if (st != TBFS_OK) return st;
+  if (undirected) build_flags |= TBFS_BUILD_SYMMETRIZE;
+  else build_flags &= ~TBFS_BUILD_SYMMETRIZE;
+  if (nz > ((build_flags & TBFS_BUILD_SYMMETRIZE) ? INT32_MAX / 2 : INT32_MAX)) {
+    tbfs_set_error("tbfs_graph_create_mm: too many entries for int32 lists");
+    return TBFS_ERR_UNSUPPORTED;
+  }
+  if ((st = need_device()) != TBFS_OK) return st;
+  const long long len = (long long)(bytes - data);
+  char *dt = nullptr;
+  int *ds = nullptr, *dd = nullptr;
+  const size_t eb = (size_t)(nz > 0 ? nz : 1) * sizeof(int);
+  cudaError_t e = cudaMalloc(&dt, (size_t)(len > 0 ? len : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&ds, eb);
+  if (e == cudaSuccess) e = cudaMalloc(&dd, eb);
+  if (e == cudaSuccess && len > 0) e = cudaMemcpy(dt, text + data, (size_t)len, cudaMemcpyHostToDevice);
+  long long lines = 0, bad = -1;
+  if (e == cudaSuccess) e = tbfs::mm_parse_device(dt, len, nz, M, N, ds, dd, &lines, &bad, 0);
+  cudaFree(dt);
+  if (e == cudaSuccess) {
+    if (lines < nz) {
+      tbfs_set_error("Matrix Market text ends after %lld of %lld entries", lines, nz);
+      st = TBFS_ERR_IO;
+    } else if (bad >= 0) {
+      tbfs_set_error("Matrix Market: bad entry line %lld", bad);
+      st = TBFS_ERR_IO;
+    } else {
+      st = graph_from_device_edges(ds, dd, (int32_t)N, nz, build_flags, graph_flags, out);
+    }
+  }
+  cudaFree(ds);
+  cudaFree(dd);
+  if (e != cudaSuccess) return cuda_fail(e, "Matrix Market parse on the device", __LINE__);
+  return st;
+}
+
+extern "C" tbfs_status tbfs_graph_load_mm(const char *path, int32_t undirected,
+                                          uint32_t build_flags, uint32_t graph_flags,
+                                          tbfs_graph **out) {
+  if (!out) return invalid("tbfs_graph_load_mm: null out pointer");
+  *out = nullptr;
+  if (!path) return invalid("tbfs_graph_load_mm: null path");
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    tbfs_set_error("tbfs_graph_load_mm: cannot open %s", path);
+    return TBFS_ERR_IO;
+  }
+  fseek(f, 0, SEEK_END);
+  const long long size = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  if (size <= 0) {
+    fclose(f);
+    tbfs_set_error("tbfs_graph_load_mm: %s is empty", path);
+    return TBFS_ERR_IO;
+  }
+  char *text = nullptr; /* pinned: the upload runs at full link speed */
+  bool pinned = true;
+  if (cudaMallocHost(&text, (size_t)size) != cudaSuccess) {
+    cudaGetLastError();
+    pinned = false;
+    text = static_cast<char *>(malloc((size_t)size));
+    if (!text) {
+      fclose(f);
+      return TBFS_ERR_OUT_OF_MEMORY;
+    }
+  }
+  const size_t got = fread(text, 1, (size_t)size, f);
+  fclose(f);
+  tbfs_status st = TBFS_ERR_IO;
+  if (got != (size_t)size)
+    tbfs_set_error("tbfs_graph_load_mm: short read of %s", path);
+  else
+    st = tbfs_graph_create_mm(text, size, undirected, build_flags, graph_flags, out);
+  if (pinned) cudaFreeHost(text);
+  else free(text);
+  return st;
+}
+
+/* The resident in-lists back in the caller's numbering: only for graphs
+ * kept in that numbering (TBFS_GRAPH_KEEP_ORDER, or a grouping that left the
+ * order unchanged). */
+extern "C" tbfs_status tbfs_graph_get_csc(const tbfs_graph *g, int32_t *col_ptr,
+                                          int32_t *row_idx) {
+  if (!g || !col_ptr || (g->nnz > 0 && !row_idx)) return invalid("tbfs_graph_get_csc: null argument");
+  if (g->inv) {
+    tbfs_set_error("tbfs_graph_get_csc: the graph is stored regrouped by degree");
+    return TBFS_ERR_UNSUPPORTED;
+  }
+  CUDA_TRY(cudaSetDevice(g->device));
+  CUDA_TRY(cudaMemcpy(col_ptr, g->cp, ((size_t)g->n + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+  if (g->nnz > 0)
+    CUDA_TRY(cudaMemcpy(row_idx, g->ic, (size_t)g->nnz * sizeof(int), cudaMemcpyDeviceToHost));
   return TBFS_OK;
 }
 

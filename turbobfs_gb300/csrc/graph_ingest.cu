@@ -5,11 +5,13 @@
  *                        for COOC -> CSC (key = column) and for the transpose
  *                        CSC -> out-lists (key = row id)
  *   expand_columns       column id of every CSC entry
+ *   stable_sort_pairs    LSD radix sort of (key, val) pairs, 8 bits a pass,
+ *                        stable: equal keys keep their input order
  * Replaces the host-side format builders of the reference
  * (TurboBFS_CSC_TD/sparseformatransf.c:28-120,
  * TurboBFS_COOC_TD/sparseformatransf.c:62-95) for graphs already on the GPU.
- * The order of entries inside a list after counting_sort_lists is not
- * deterministic; BFS depth and path counts do not depend on it.
+ * counting_sort_lists is stable too, so a list keeps the input order of its
+ * entries: a COOC list the file order, a transposed list ascending columns.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -53,19 +55,6 @@ __global__ void histogram_kernel(const int *keys, long long nnz, int n, int *cnt
   }
 }
 
-__global__ void scatter_kernel(const int *keys, const int *vals, long long nnz, int n,
-                               int *fill, int *idx, int *flag) {
-  for (unsigned long long k = gtid(); k < (unsigned long long)nnz; k += gstride()) {
-    const int key = keys[k], val = vals[k];
-    if (key < 0 || key >= n || val < 0 || val >= n) {
-      atomicOr(flag, 2);
-      continue;
-    }
-    const int pos = atomicAdd(fill + key, 1);
-    idx[pos] = val;
-  }
-}
-
 /* one warp per column writes the column id over its entry range */
 __global__ void expand_kernel(const int *cp, int n, int *col) {
   const unsigned lane = threadIdx.x & 31;
@@ -73,6 +62,80 @@ __global__ void expand_kernel(const int *cp, int n, int *col) {
   for (unsigned long long v = w0; v < (unsigned long long)n; v += nw) {
     const int b = cp[v], e = cp[v + 1];
     for (int k = b + (int)lane; k < e; k += 32) col[k] = (int)v;
+  }
+}
+
+/* ---- stable LSD radix sort of (key, val) pairs ----
+ * A pass sorts by the 8-bit digit (key >> shift) & 255.  Tiles of kRadixTile
+ * consecutive pairs; hist[d * ntiles + t] counts digit d in tile t, and its
+ * exclusive scan (digit-major) is where tile t's pairs of digit d start.
+ * The scatter re-reads each tile in order -- warp w its 512-pair slice, 32
+ * pairs a round -- and ranks equal digits by lane (match_any), so the output
+ * keeps the input order among equal digits. */
+constexpr int kRadixTile = 4096;
+constexpr int kRadixWarpSlice = kRadixTile / (kThreads / 32);
+
+__global__ void radix_hist_kernel(const unsigned *keys, long long len, int shift, int ntiles,
+                                  int *hist) {
+  __shared__ int h[256];
+  for (int i = threadIdx.x; i < 256; i += kThreads) h[i] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kRadixTile;
+  for (int i = threadIdx.x; i < kRadixTile; i += kThreads) {
+    const long long j = base + i;
+    if (j < len) atomicAdd(&h[(keys[j] >> shift) & 255u], 1);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += kThreads) hist[(long long)d * ntiles + blockIdx.x] = h[d];
+}
+
+__global__ void radix_scatter_kernel(const unsigned *keys, const unsigned *vals, long long len,
+                                     int shift, int ntiles, const int *offs, unsigned *ko,
+                                     unsigned *vo) {
+  static_assert(kThreads == 256, "one thread per digit in the warp prefix");
+  __shared__ int cnt[kThreads / 32][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const long long base = (long long)blockIdx.x * kRadixTile + (long long)w * kRadixWarpSlice;
+  for (int d = lane; d < 256; d += 32) cnt[w][d] = 0;
+  __syncwarp();
+  for (int r = 0; r < kRadixWarpSlice / 32; ++r) { /* digit counts of the warp's slice */
+    const long long j = base + r * 32 + lane;
+    const bool ok = j < len;
+    const unsigned d = ok ? (keys[j] >> shift) & 255u : 256u + (unsigned)lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (ok && (peers & lt) == 0u) cnt[w][d] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  { /* start of each warp's digit d: the tile's start + earlier warps' counts */
+    const int d = threadIdx.x;
+    int run = offs[(long long)d * ntiles + blockIdx.x];
+    for (int ww = 0; ww < kThreads / 32; ++ww) {
+      const int c = cnt[ww][d];
+      cnt[ww][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  for (int r = 0; r < kRadixWarpSlice / 32; ++r) {
+    const long long j = base + r * 32 + lane;
+    const bool ok = j < len;
+    unsigned k = 0, v = 0;
+    if (ok) {
+      k = keys[j];
+      v = vals[j];
+    }
+    const unsigned d = ok ? (k >> shift) & 255u : 256u + (unsigned)lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (ok) {
+      const int pos = cnt[w][d] + __popc(peers & lt);
+      ko[pos] = k;
+      vo[pos] = v;
+    }
+    __syncwarp();
+    if (ok && (peers & lt) == 0u) cnt[w][d] += __popc(peers);
+    __syncwarp();
   }
 }
 
@@ -188,6 +251,45 @@ cudaError_t validate_csc(const int *cp, const int *ic, int n, long long nnz, int
   return cudaGetLastError();
 }
 
+int key_bits(unsigned max_key) {
+  int b = 0;
+  while (b < 32 && (max_key >> b) != 0u) ++b;
+  return b;
+}
+
+cudaError_t stable_sort_pairs(unsigned *keys, unsigned *vals, long long len, int bits,
+                              unsigned *ktmp, unsigned *vtmp, cudaStream_t s) {
+  if (len <= 1 || bits <= 0) return cudaSuccess;
+  const long long tiles = (len + kRadixTile - 1) / kRadixTile;
+  if (tiles * 256 > INT32_MAX) return cudaErrorInvalidValue;
+  int *hist = nullptr;
+  cudaError_t e = cudaMalloc(&hist, (size_t)tiles * 256 * sizeof(int));
+  if (e != cudaSuccess) return e;
+  unsigned *ka = keys, *va = vals, *kb = ktmp, *vb = vtmp;
+  for (int shift = 0; shift < bits && e == cudaSuccess; shift += 8) {
+    radix_hist_kernel<<<(unsigned)tiles, kThreads, 0, s>>>(ka, len, shift, (int)tiles, hist);
+    if ((e = cudaGetLastError()) != cudaSuccess) break;
+    if ((e = exclusive_scan(hist, tiles * 256, hist, s)) != cudaSuccess) break;
+    radix_scatter_kernel<<<(unsigned)tiles, kThreads, 0, s>>>(ka, va, len, shift, (int)tiles, hist,
+                                                              kb, vb);
+    e = cudaGetLastError();
+    unsigned *t = ka;
+    ka = kb;
+    kb = t;
+    t = va;
+    va = vb;
+    vb = t;
+  }
+  if (e == cudaSuccess && ka != keys) { /* odd number of passes: back to the caller's buffers */
+    e = cudaMemcpyAsync(keys, ka, (size_t)len * sizeof(unsigned), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(vals, va, (size_t)len * sizeof(unsigned), cudaMemcpyDeviceToDevice, s);
+  }
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaFree(hist);
+  return e != cudaSuccess ? e : e2;
+}
+
 cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz, int n,
                                 int *ptr_out, int *idx_out, int *d_flag, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(ptr_out, 0, ((size_t)n + 1) * sizeof(int), s);
@@ -195,15 +297,29 @@ cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
   histogram_kernel<<<grid_for(nnz), kThreads, 0, s>>>(keys, nnz, n, ptr_out, d_flag);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if ((e = exclusive_scan(ptr_out, (long long)n + 1, ptr_out, s)) != cudaSuccess) return e;
-  int *fill = nullptr;
-  if ((e = cudaMalloc(&fill, ((size_t)n + 1) * sizeof(int))) != cudaSuccess) return e;
-  e = cudaMemcpyAsync(fill, ptr_out, ((size_t)n + 1) * sizeof(int), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess) {
-    scatter_kernel<<<grid_for(nnz), kThreads, 0, s>>>(keys, vals, nnz, n, fill, idx_out, d_flag);
+  int flag = 0;
+  if ((e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  if (flag) return cudaSuccess; /* a key out of range: the caller reports it */
+  /* stable: sort copies of the pairs by key, the values are the lists */
+  const size_t m = (size_t)(nnz > 0 ? nnz : 1);
+  unsigned *buf = nullptr;
+  if ((e = cudaMalloc(&buf, 4 * m * sizeof(unsigned))) != cudaSuccess) return e;
+  unsigned *k = buf, *v = buf + m, *kt = buf + 2 * m, *vt = buf + 3 * m;
+  e = cudaMemcpyAsync(k, keys, (size_t)nnz * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(v, vals, (size_t)nnz * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess)
+    e = stable_sort_pairs(k, v, nnz, key_bits((unsigned)(n > 0 ? n - 1 : 0)), kt, vt, s);
+  if (e == cudaSuccess && nnz)
+    e = cudaMemcpyAsync(idx_out, v, (size_t)nnz * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) { /* values out of range */
+    validate_kernel<<<grid_for(nnz), kThreads, 0, s>>>(ptr_out, idx_out, n, nnz, d_flag);
     e = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamSynchronize(s);
-  cudaFree(fill);
+  cudaFree(buf);
   return e != cudaSuccess ? e : e2;
 }
 

@@ -222,9 +222,33 @@ cudaError_t multi_gather(const int *S, const unsigned long long *sig, const int 
 /* graph ingest helpers (graph_ingest.cu) */
 cudaError_t validate_csc(const int *cp, const int *ic, int n, long long nnz,
                          int *d_flag, cudaStream_t s);
+/* (key, val) pairs -> ptr[n+1] / idx[nnz] lists, each list in the input
+ * order of its entries; a key outside [0, n) sets bit 2 of *d_flag (and the
+ * lists are then not built), a value outside it too */
 cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
                                 int n, int *ptr_out, int *idx_out, int *d_flag,
                                 cudaStream_t s);
+/* stable LSD radix sort of len (key, val) pairs by the low `bits` bits of
+ * the key; ktmp / vtmp are len-element scratch; synchronises s */
+cudaError_t stable_sort_pairs(unsigned *keys, unsigned *vals, long long len, int bits,
+                              unsigned *ktmp, unsigned *vtmp, cudaStream_t s);
+/* bits needed for keys up to max_key */
+int key_bits(unsigned max_key);
+
+/* device edge list -> CSC (cp[n+1], ic[nnz], allocated here) with the host
+ * builder's construction flags (TBFS_BUILD_*); *bad = 1 when an endpoint is
+ * outside [0, n).  cudaErrorInvalidValue: more than INT32_MAX pairs.
+ * (mm_ingest.cu) */
+cudaError_t csc_from_edges_device(const int *src, const int *dst, long long m, int n,
+                                  unsigned flags, int **cp_out, int **ic_out, long long *nnz_out,
+                                  int *bad_out, cudaStream_t s);
+/* the data lines of a Matrix Market coordinate file (len bytes on the
+ * device, starting at a line) -> src/dst of the first nz entries;
+ * *lines = data lines found, *bad = first entry that is not two indices in
+ * range (or -1) */
+cudaError_t mm_parse_device(const char *text, long long len, long long nz, long long M,
+                            long long N, int *src, int *dst, long long *lines_out,
+                            long long *bad_out, cudaStream_t s);
 /* exclusive prefix sum of len ints (in place allowed); synchronises s */
 cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t s);
 cudaError_t expand_columns(const int *cp, int n, int *col_of_entry, cudaStream_t s);
