@@ -2,9 +2,11 @@
 oracle's restatement of the same summation order.
 
 Bar: bit-exact (float64 compared with ==) on graphs whose out-lists are the
-caller's CSC (symmetric graphs), in both vertex numberings; to 1e-12
-relative on directed graphs, whose device-built out-lists have no fixed
-order."""
+caller's CSC (symmetric graphs), in both vertex numberings, and on directed
+graphs kept in the caller's numbering (the device transpose lists each
+out-list by ascending column, as the oracle does); to 1e-12 relative on
+directed graphs regrouped by degree, whose out-lists follow the new
+numbering."""
 import numpy as np
 import pytest
 
@@ -64,6 +66,11 @@ def test_brandes_directed_to_rounding(gpu_available):
     with tb.Graph.from_host_csc(h) as g:
         bc, _ = g.betweenness(roots)
     np.testing.assert_allclose(bc, want, rtol=1e-12, atol=1e-9)
+    # in the caller's numbering the device transpose lists each out-list by
+    # ascending column, the oracle's order: the same sums, bit for bit
+    with tb.Graph.from_host_csc(h, keep_order=True) as gk:
+        bck, _ = gk.betweenness(roots)
+    assert np.array_equal(bck, want)
 
 
 def test_brandes_all_roots_small_and_invalid(gpu_available):
