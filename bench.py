@@ -59,12 +59,15 @@ def parse_args():
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-autotune", action="store_true",
                    help="default alpha/beta/pull_ratio instead of the autotuned ones")
-    p.add_argument("--part", choices=["all", "batched", "serving", "ingest"], default="all",
-                   help="batched / serving / ingest: run only that report and print it")
+    p.add_argument("--part", choices=["all", "batched", "serving", "ingest", "brandes"],
+                   default="all", help="run only that report and print it")
     p.add_argument("--no-batched", action="store_true", help="skip the batched report")
     p.add_argument("--no-serving", action="store_true", help="skip the serving report")
     p.add_argument("--no-ingest", action="store_true", help="skip the ingest report")
     p.add_argument("--ingest-scale", type=int, default=21)
+    p.add_argument("--no-brandes", action="store_true", help="skip the betweenness report")
+    p.add_argument("--brandes-scale", type=int, default=20)
+    p.add_argument("--brandes-roots", type=int, default=16)
     p.add_argument("--batch-scale", type=int, default=20)
     p.add_argument("--batch-roots", type=int, default=256)
     p.add_argument("--arena-graphs", type=int, default=512)
@@ -367,6 +370,8 @@ def run_tbfs(args, world, rank, local):
         line["serving"] = serving_report(args)
     if rank == 0 and world == 1 and not args.no_ingest:
         line["ingest"] = ingest_report(args)
+    if rank == 0 and world == 1 and not args.no_brandes:
+        line["brandes"] = brandes_report(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
@@ -787,6 +792,44 @@ def ingest_report(args):
                       "graph; host path = tbfs_mm_read + tbfs_graph_create_csc"}
 
 
+def brandes_report(args):
+    """Betweenness (forward traversal + dependency sweep per root) on RMAT:
+    device time per root through tbfs_brandes, against the oracle's
+    single-threaded restatement of the same computation (the CPU baseline,
+    also the bit-exact checker) on two of the roots."""
+    import oracle
+    import turbobfs_gb300 as tb
+    from turbobfs_gb300 import graphs
+
+    scale, k = args.brandes_scale, args.brandes_roots
+    h = graphs.rmat(scale, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    roots = graphs.pick_roots(h, k, seed=3)
+    with tb.Graph.from_host_csc(h) as g:
+        g.betweenness(roots[:2])  # warm-up
+        t0 = time.perf_counter()
+        bc, ovf = g.betweenness(roots)
+        gpu_s = time.perf_counter() - t0
+        bc2, _ = g.betweenness(roots[:2])
+    t1 = time.perf_counter()
+    want, _ = oracle.brandes(h.col_ptr, h.row_idx, roots[:2])
+    cpu_s = time.perf_counter() - t1
+    deg = np.diff(h.col_ptr).astype(np.int64)
+    S, _, _, _ = oracle.exact_bfs(h.col_ptr, h.row_idx, int(roots[0]))
+    m_c = int(deg[S >= 0].sum()) // 2
+    return {"workload": f"RMAT scale {scale}, edgefactor 16, {k} roots from the giant component, "
+                        "unnormalised betweenness (S, sigma forward + Brandes sweep per root)",
+            "n": int(h.n), "nnz": int(h.nnz), "roots": k, "component_edges": m_c,
+            "gpu_ms_per_root": gpu_s * 1e3 / k,
+            "gpu_gteps": 2 * m_c * k / gpu_s / 1e9,
+            "cpu_baseline": {"ms_per_root": cpu_s * 1e3 / 2, "cores": 1, "kind": "port",
+                             "sample": "2 of the roots, one thread (oracle_brandes)"},
+            "speedup_vs_cpu": (cpu_s / 2) / (gpu_s / k),
+            "bit_identical_to_oracle": bool(np.array_equal(bc2, want)),
+            "sigma_overflow_roots": int(ovf),
+            "metric_note": "gteps counts each component edge twice per root (forward and sweep); "
+                           "host wall clock around tbfs_brandes"}
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_env()
@@ -797,7 +840,7 @@ def main():
 
         torch.cuda.set_device(local)
         rep = {"batched": batched_report, "serving": serving_report,
-               "ingest": ingest_report}[args.part](args)
+               "ingest": ingest_report, "brandes": brandes_report}[args.part](args)
         print(json.dumps({"part": args.part, args.part: rep}), flush=True)
         return 0
     return run_tbfs(args, world, rank, local)

@@ -506,11 +506,15 @@ double oracle_seq_many(const int *IC, const int *CP, int nz, int n,
  * library's GPU sweep so that results can be compared bit for bit:
  * delta[v] sums sigma[v]/sigma[w] * (1 + delta[w]) over the out-list
  * entries v -> w with S[w] = S[v] + 1; below 32 entries in list order,
- * otherwise 32 strided partial sums (entries l, l+32, ...) combined by a
- * butterfly (xor 16, 8, 4, 2, 1).  Built with -ffp-contract=off so that
+ * otherwise per segment of BRANDES_SEG entries 32 strided partial sums
+ * (entries l, l+32, ...) combined by a butterfly (xor 16, 8, 4, 2, 1), the
+ * segment sums added in segment order.  Built with -ffp-contract=off so that
  * no multiply-add is fused.  (orp, ojr): out-lists; bc accumulates over
  * the roots in order; returns the number of roots whose counts wrapped.
  * ------------------------------------------------------------------ */
+/* segment length of the dependency sums of lists of 32 entries or more */
+#define BRANDES_SEG 2048
+
 int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int k, double *bc) {
   int *S = (int *)malloc((size_t)n * sizeof(int));
   uint64_t *sg = (uint64_t *)malloc((size_t)n * sizeof(uint64_t));
@@ -560,26 +564,29 @@ int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int 
             acc = acc + term;
           }
         }
-      } else {
-        double part[32], nxt[32];
-        for (int l = 0; l < 32; ++l) {
-          double a = 0.0;
-          for (int j = b + l; j < e; j += 32) {
-            const int w = ojr[j];
-            if (S[w] == d + 1) {
-              const double c = sv / (double)sg[w];
-              const double t = 1.0 + delta[w];
-              const double term = c * t;
-              a = a + term;
+      } else { /* segments of BRANDES_SEG entries, their sums in order */
+        for (int sb = b; sb < e; sb += BRANDES_SEG) {
+          const int se = sb + BRANDES_SEG < e ? sb + BRANDES_SEG : e;
+          double part[32], nxt[32];
+          for (int l = 0; l < 32; ++l) {
+            double a = 0.0;
+            for (int j = sb + l; j < se; j += 32) {
+              const int w = ojr[j];
+              if (S[w] == d + 1) {
+                const double c = sv / (double)sg[w];
+                const double t = 1.0 + delta[w];
+                const double term = c * t;
+                a = a + term;
+              }
             }
+            part[l] = a;
           }
-          part[l] = a;
+          for (int o = 16; o > 0; o >>= 1) {
+            for (int l = 0; l < 32; ++l) nxt[l] = part[l] + part[l ^ o];
+            memcpy(part, nxt, sizeof(part));
+          }
+          acc = sb == b ? part[0] : acc + part[0];
         }
-        for (int o = 16; o > 0; o >>= 1) {
-          for (int l = 0; l < 32; ++l) nxt[l] = part[l] + part[l ^ o];
-          memcpy(part, nxt, sizeof(part));
-        }
-        acc = part[0];
       }
       delta[v] = acc;
       if (v != r) bc[v] = bc[v] + acc;

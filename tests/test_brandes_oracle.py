@@ -63,3 +63,22 @@ def test_oracle_brandes_subset_of_roots_and_star():
     # from each leaf root, the centre carries the 48 other leaves
     assert bc[0] == 3 * (n - 2)
     assert np.all(bc[1:] == 0)
+
+
+def test_oracle_brandes_hub_segments_match_networkx():
+    # a hub of out-degree 6000 (three segments of the summation order) on
+    # top of a sparse random graph
+    rng = np.random.default_rng(8)
+    n = 6500
+    src = np.concatenate([np.zeros(6000, np.int32), rng.integers(1, n, 9000, dtype=np.int32)])
+    dst = np.concatenate([np.arange(1, 6001, dtype=np.int32), rng.integers(1, n, 9000, dtype=np.int32)])
+    h = graphs.from_edges(n, src, dst, symmetrize=True, dedup=True, drop_loops=True)
+    assert np.diff(h.col_ptr).max() > 2 * 2048
+    nx, G = _nx_graph(h, directed=False)
+    roots = np.arange(0, n, 97, dtype=np.int32)
+    bc, _ = oracle.brandes(h.col_ptr, h.row_idx, roots)
+    ref = nx.betweenness_centrality_subset(G, sources=roots.tolist(), targets=list(range(n)),
+                                           normalized=False)
+    # subset betweenness counts each (source, target) pair once, halved for
+    # undirected graphs; the sweep counts it once per source
+    np.testing.assert_allclose(bc, 2.0 * np.array([ref[v] for v in range(n)]), rtol=1e-9, atol=1e-7)

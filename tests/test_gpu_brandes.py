@@ -32,10 +32,19 @@ def test_brandes_fixtures_bit_exact(gpu_available, name):
     assert np.array_equal(bc, want)
 
 
-@pytest.mark.parametrize("kind", ["er", "rmat12", "rmat16", "grid"])
+@pytest.mark.parametrize("kind", ["er", "rmat12", "rmat16", "grid", "hub"])
 def test_brandes_synthetic_bit_exact_both_numberings(gpu_available, kind):
     if kind == "er":
         h = graphs.erdos_renyi(20000, 80000, seed=3)
+    elif kind == "hub":  # lists of 6000 and 12000 entries: segmented sums
+        rng = np.random.default_rng(4)
+        n = 20000
+        src = np.concatenate([np.zeros(6000, np.int32), np.ones(12000, np.int32),
+                              rng.integers(2, n, 40000, dtype=np.int32)])
+        dst = np.concatenate([np.arange(2, 6002, dtype=np.int32),
+                              np.arange(3000, 15000, dtype=np.int32),
+                              rng.integers(2, n, 40000, dtype=np.int32)])
+        h = graphs.from_edges(n, src, dst, symmetrize=True, dedup=True, drop_loops=True)
     elif kind == "rmat12":
         h = graphs.rmat(12, 16, seed=3)
     elif kind == "rmat16":

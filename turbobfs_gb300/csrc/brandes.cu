@@ -14,8 +14,13 @@
  * Every delta is a pull over the vertex's own out-list in a fixed order, so
  * the result does not depend on scheduling:
  *   out-degree < 32: one lane sums the terms in list order;
- *   otherwise: lane l sums the entries l, l+32, l+64, ... in order, then the
- *   32 partial sums meet in a butterfly (xor 16, 8, 4, 2, 1).
+ *   otherwise the list is cut into segments of kSeg entries (one segment up
+ *   to kSeg); in a segment, lane l sums the entries l, l+32, l+64, ... in
+ *   order and the 32 partial sums meet in a butterfly (xor 16, 8, 4, 2, 1);
+ *   the segments' sums are added in segment order.
+ * A hub's segments are separate work items of the level, so a list of 10^5
+ * entries is summed by tens of warps at once; its segment sums are combined
+ * after a grid barrier.
  * Terms are (double)sigma[v] / (double)sigma[w] * (1 + delta[w]) with
  * correctly rounded IEEE operations and no contraction into fused
  * multiply-adds, so a CPU restatement of the same order reproduces every
@@ -39,6 +44,7 @@ constexpr int kBlock = 256;
 constexpr int kSmemLevels = 8192; /* levels counted in shared memory per block */
 constexpr int kTile = 4096;       /* vertices per block of the counting sort   */
 constexpr int kWarpDegree = 32;   /* out-degree from which a warp sums a vertex */
+constexpr int kSeg = 2048;        /* entries per segment of a hub's list        */
 
 struct __align__(128) SweepCtl {
   int status, timeout_level;
@@ -57,6 +63,12 @@ struct SweepParams {
   const int *inv;                    /* ... mapped by inv (or null)          */
   double *delta;                     /* n, zero on entry                     */
   double *bc;                        /* n, accumulated                       */
+  /* hubs (out-degree > kSeg) by list position i: segoff[i] (exclusive prefix
+   * of their segment counts over positions), hoff[i] (of the hub flags);
+   * hubpos[h] = position of hub h, seg_hub[s] = hub of segment s,
+   * part[s] = sum of segment s */
+  const int *segoff, *hoff, *hubpos, *seg_hub;
+  double *part;
   SweepCtl *ctl;
   long long timeout_ns;
 };
@@ -93,45 +105,103 @@ __device__ __forceinline__ double sum_entries(const SweepParams &p, int d, doubl
   return acc;
 }
 
+/* the terms of [b, e) summed lane-strided over the warp, then the butterfly;
+ * every lane returns the same value (lane 0's order) */
+__device__ __forceinline__ double warp_sum(const SweepParams &p, int d, double sv, int b, int e) {
+  const int lane = threadIdx.x & 31;
+  double acc = sum_entries(p, d, sv, b + lane, e, 32);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(FULL, acc, o));
+  return __shfl_sync(FULL, acc, 0);
+}
+
 __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
   const int lane = threadIdx.x & 31;
   const int root = p.inv ? __ldg(p.inv + p.root) : p.root;
   const unsigned gwarp = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const unsigned nwarps = (gridDim.x * kBlock) >> 5;
+  const unsigned gthread = blockIdx.x * kBlock + threadIdx.x;
   for (int d = p.levels - 2; d >= 0; --d) {
     const int lo = __ldg(p.off + d), hi = __ldg(p.off + d + 1);
-    /* chunks of 32 vertices of level d per warp */
-    for (int base = lo + (int)gwarp * 32; base < hi; base += (int)nwarps * 32) {
-      const int i = base + lane;
-      int v = -1, b = 0, e = 0;
-      if (i < hi) {
-        v = __ldg(p.list + i);
-        b = __ldg(p.rp + v);
-        e = __ldg(p.rp + v + 1);
+    const int s_lo = __ldg(p.segoff + lo), s_hi = __ldg(p.segoff + hi);
+    const int h_lo = __ldg(p.hoff + lo), h_hi = __ldg(p.hoff + hi);
+    const unsigned nch = (unsigned)(hi - lo + 31) / 32u;
+    const unsigned items = nch + (unsigned)(s_hi - s_lo);
+    /* items: chunks of 32 vertices of level d, then the hubs' segments */
+    for (unsigned it = gwarp; it < items; it += nwarps) {
+      if (it < nch) {
+        const int i = lo + (int)it * 32 + lane;
+        int v = -1, b = 0, e = 0;
+        if (i < hi) {
+          v = __ldg(p.list + i);
+          b = __ldg(p.rp + v);
+          e = __ldg(p.rp + v + 1);
+        }
+        const bool heavy = v >= 0 && e - b >= kWarpDegree && e - b <= kSeg;
+        if (v >= 0 && e - b < kWarpDegree) {
+          const double acc = sum_entries(p, d, (double)__ldg(p.sig + v), b, e, 1);
+          p.delta[v] = acc;
+          if (v != root) p.bc[v] = __dadd_rn(p.bc[v], acc);
+        }
+        /* one-segment lists of the chunk, one at a time with the whole warp */
+        unsigned hv = __ballot_sync(FULL, heavy);
+        while (hv) {
+          const int src = __ffs(hv) - 1;
+          hv &= hv - 1u;
+          const int vv = __shfl_sync(FULL, v, src);
+          const int bb = __shfl_sync(FULL, b, src), ee = __shfl_sync(FULL, e, src);
+          const double acc = warp_sum(p, d, (double)__ldg(p.sig + vv), bb, ee);
+          if (lane == 0) {
+            p.delta[vv] = acc;
+            if (vv != root) p.bc[vv] = __dadd_rn(p.bc[vv], acc);
+          }
+        }
+      } else { /* segment s of a hub */
+        const int sg = s_lo + (int)(it - nch);
+        const int i = __ldg(p.hubpos + __ldg(p.seg_hub + sg));
+        const int v = __ldg(p.list + i);
+        const int b = __ldg(p.rp + v) + (sg - __ldg(p.segoff + i)) * kSeg;
+        const int e = min(b + kSeg, __ldg(p.rp + v + 1));
+        const double acc = warp_sum(p, d, (double)__ldg(p.sig + v), b, e);
+        if (lane == 0) p.part[sg] = acc;
       }
-      const bool heavy = v >= 0 && e - b >= kWarpDegree;
-      if (v >= 0 && !heavy) {
-        const double acc = sum_entries(p, d, (double)__ldg(p.sig + v), b, e, 1);
+    }
+    if (h_hi > h_lo) { /* the hubs of level d: their segments in order */
+      if (!grid_barrier(p.ctl, p.timeout_ns, d)) return;
+      for (unsigned t = gthread; t < (unsigned)(h_hi - h_lo); t += gridDim.x * kBlock) {
+        const int i = __ldg(p.hubpos + h_lo + (int)t);
+        const int v = __ldg(p.list + i);
+        const int s0 = __ldg(p.segoff + i), s1 = __ldg(p.segoff + i + 1);
+        double acc = __ldcg(p.part + s0);
+        for (int sg = s0 + 1; sg < s1; ++sg) acc = __dadd_rn(acc, __ldcg(p.part + sg));
         p.delta[v] = acc;
         if (v != root) p.bc[v] = __dadd_rn(p.bc[v], acc);
       }
-      /* heavy vertices of the chunk, one at a time with the whole warp */
-      unsigned hv = __ballot_sync(FULL, heavy);
-      while (hv) {
-        const int src = __ffs(hv) - 1;
-        hv &= hv - 1u;
-        const int vv = __shfl_sync(FULL, v, src);
-        const int bb = __shfl_sync(FULL, b, src), ee = __shfl_sync(FULL, e, src);
-        double acc = sum_entries(p, d, (double)__ldg(p.sig + vv), bb + lane, ee, 32);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(FULL, acc, o));
-        if (lane == 0) {
-          p.delta[vv] = acc;
-          if (vv != root) p.bc[vv] = __dadd_rn(p.bc[vv], acc);
-        }
-      }
     }
     if (!grid_barrier(p.ctl, p.timeout_ns, d)) return;
+  }
+}
+
+/* segs[i] = segments of the vertex at list position i (0 unless a hub),
+ * flag[i] = it is a hub; i < cnt */
+__global__ void hub_count_kernel(const int *list, const int *rp, int cnt, int *segs, int *flag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const int v = list[i];
+    const int deg = rp[v + 1] - rp[v];
+    const int h = deg > kSeg ? 1 : 0;
+    segs[i] = h ? (deg + kSeg - 1) / kSeg : 0;
+    flag[i] = h;
+  }
+}
+
+/* hubpos[hoff[i]] = i and seg_hub[s] = hoff[i] for the hubs' segments */
+__global__ void hub_fill_kernel(const int *segoff, const int *hoff, int cnt, int *hubpos,
+                                int *seg_hub) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const int h = hoff[i];
+    if (hoff[i + 1] == h) continue;
+    hubpos[h] = i;
+    for (int sg = segoff[i]; sg < segoff[i + 1]; ++sg) seg_hub[sg] = h;
   }
 }
 
@@ -224,6 +294,9 @@ tbfs_status bfail(cudaError_t e, const char *what) {
 
 struct Scratch {
   int *S = nullptr, *list = nullptr, *off = nullptr, *fill = nullptr;
+  int *segoff = nullptr, *hoff = nullptr, *hubpos = nullptr, *seg_hub = nullptr;
+  double *part = nullptr;
+  long long part_cap = 0;
   unsigned long long *sig = nullptr;
   double *delta = nullptr, *bc = nullptr, *out = nullptr;
   SweepCtl *ctl = nullptr;
@@ -234,6 +307,11 @@ struct Scratch {
     cudaFree(list);
     cudaFree(off);
     cudaFree(fill);
+    cudaFree(segoff);
+    cudaFree(hoff);
+    cudaFree(hubpos);
+    cudaFree(seg_hub);
+    cudaFree(part);
     cudaFree(sig);
     cudaFree(delta);
     cudaFree(bc);
@@ -269,6 +347,9 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
   BTRY(cudaMalloc(&w.list, n * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.off, (n + 2) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.fill, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.segoff, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.hoff, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.hubpos, (n + 1) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.delta, n * sizeof(double)), "alloc");
   BTRY(cudaMalloc(&w.bc, n * sizeof(double)), "alloc");
   BTRY(cudaMalloc(&w.ctl, sizeof(SweepCtl)), "alloc");
@@ -310,6 +391,36 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
          "fill pointers");
     tbfs::level_fill_kernel<<<tiles, tbfs::kBlock, 0, s>>>(w.S, g->n, levels, w.fill, w.list);
     BTRY(cudaGetLastError(), "level fill");
+    /* hubs: segment counts and flags by list position, their prefixes, the
+     * hub and segment maps */
+    int reached = 0;
+    BTRY(cudaMemcpyAsync(&reached, w.off + levels, sizeof(int), cudaMemcpyDeviceToHost, s),
+         "reached");
+    BTRY(cudaStreamSynchronize(s), "reached");
+    const unsigned cgrid = (unsigned)((reached + 255) / 256 > 0 ? (reached + 255) / 256 : 1);
+    BTRY(cudaMemsetAsync(w.segoff + reached, 0, sizeof(int), s), "clear");
+    BTRY(cudaMemsetAsync(w.hoff + reached, 0, sizeof(int), s), "clear");
+    tbfs::hub_count_kernel<<<cgrid, 256, 0, s>>>(w.list, g->rp, reached, w.segoff, w.hoff);
+    BTRY(cudaGetLastError(), "hub count");
+    BTRY(tbfs::exclusive_scan(w.segoff, (long long)reached + 1, w.segoff, s), "segment prefix");
+    BTRY(tbfs::exclusive_scan(w.hoff, (long long)reached + 1, w.hoff, s), "hub prefix");
+    int nseg = 0;
+    BTRY(cudaMemcpyAsync(&nseg, w.segoff + reached, sizeof(int), cudaMemcpyDeviceToHost, s),
+         "segments");
+    BTRY(cudaStreamSynchronize(s), "segments");
+    if (nseg > w.part_cap) {
+      cudaFree(w.part);
+      cudaFree(w.seg_hub);
+      w.part = nullptr;
+      w.seg_hub = nullptr;
+      BTRY(cudaMalloc(&w.part, (size_t)nseg * sizeof(double)), "alloc");
+      BTRY(cudaMalloc(&w.seg_hub, (size_t)nseg * sizeof(int)), "alloc");
+      w.part_cap = nseg;
+    }
+    if (nseg > 0) {
+      tbfs::hub_fill_kernel<<<cgrid, 256, 0, s>>>(w.segoff, w.hoff, reached, w.hubpos, w.seg_hub);
+      BTRY(cudaGetLastError(), "hub fill");
+    }
     BTRY(cudaMemsetAsync(w.delta, 0, n * sizeof(double), s), "clear");
     BTRY(cudaMemsetAsync(w.ctl, 0, sizeof(SweepCtl), s), "clear");
     SweepParams p;
@@ -324,6 +435,11 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
     p.inv = g->inv;
     p.delta = w.delta;
     p.bc = w.bc;
+    p.segoff = w.segoff;
+    p.hoff = w.hoff;
+    p.hubpos = w.hubpos;
+    p.seg_hub = w.seg_hub;
+    p.part = w.part;
     p.ctl = w.ctl;
     p.timeout_ns = timeout;
     void *args[] = {&p};
