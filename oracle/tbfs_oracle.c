@@ -504,8 +504,9 @@ double oracle_seq_many(const int *IC, const int *CP, int nz, int n,
  * U. Brandes, J. Math. Sociology 25(2), 2001, on top of the reference's
  * forward quantities S and sigma).  Restates the summation order of the
  * library's GPU sweep so that results can be compared bit for bit:
- * delta[v] sums sigma[v]/sigma[w] * (1 + delta[w]) over the out-list
- * entries v -> w with S[w] = S[v] + 1; below 32 entries in list order,
+ * delta[v] = sigma[v] * sum of q[w] = (1 + delta[w]) / sigma[w] over the
+ * out-list entries v -> w with S[w] = S[v] + 1 (Brandes' sum with sigma[v]
+ * factored out); the sum below 32 entries in list order,
  * otherwise per segment of BRANDES_SEG entries 32 strided partial sums
  * (entries l, l+32, ...) combined by a butterfly (xor 16, 8, 4, 2, 1), the
  * segment sums added in segment order.  Built with -ffp-contract=off so that
@@ -553,16 +554,11 @@ int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int 
       const int v = q[i];
       const int d = S[v], b = orp[v], e = orp[v + 1];
       const double sv = (double)sg[v];
-      double acc = 0.0;
+      double acc = 0.0; /* sum of the children's q = (1 + delta) / sigma */
       if (e - b < 32) {
         for (int j = b; j < e; ++j) {
           const int w = ojr[j];
-          if (S[w] == d + 1) {
-            const double c = sv / (double)sg[w];
-            const double t = 1.0 + delta[w];
-            const double term = c * t;
-            acc = acc + term;
-          }
+          if (S[w] == d + 1) acc = acc + delta[w];
         }
       } else { /* segments of BRANDES_SEG entries, their sums in order */
         for (int sb = b; sb < e; sb += BRANDES_SEG) {
@@ -572,12 +568,7 @@ int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int 
             double a = 0.0;
             for (int j = sb + l; j < se; j += 32) {
               const int w = ojr[j];
-              if (S[w] == d + 1) {
-                const double c = sv / (double)sg[w];
-                const double t = 1.0 + delta[w];
-                const double term = c * t;
-                a = a + term;
-              }
+              if (S[w] == d + 1) a = a + delta[w];
             }
             part[l] = a;
           }
@@ -588,8 +579,9 @@ int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int 
           acc = sb == b ? part[0] : acc + part[0];
         }
       }
-      delta[v] = acc;
-      if (v != r) bc[v] = bc[v] + acc;
+      const double dv = sv * acc;
+      delta[v] = (1.0 + dv) / sv; /* q[v], what its parents add */
+      if (v != r) bc[v] = bc[v] + dv;
     }
   }
   free(S);

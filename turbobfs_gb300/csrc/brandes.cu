@@ -6,7 +6,10 @@
  *
  *   delta[v] = sum over out-list entries v -> w with S[w] = S[v] + 1 of
  *              sigma[v] / sigma[w] * (1 + delta[w]),
- *   bc[v]   += delta[v] for every root s != v.
+ *   bc[v]   += delta[v] for every root s != v,
+ * computed in the factored form delta[v] = sigma[v] * sum q[w] with
+ * q[w] = (1 + delta[w]) / sigma[w], stored once w is final: one division
+ * per vertex instead of one per entry, and one gather per entry.
  *
  * The sweep runs level by level from the deepest level up, as one
  * persistent cooperative launch per root with a grid barrier between levels.
@@ -21,10 +24,9 @@
  * A hub's segments are separate work items of the level, so a list of 10^5
  * entries is summed by tens of warps at once; its segment sums are combined
  * after a grid barrier.
- * Terms are (double)sigma[v] / (double)sigma[w] * (1 + delta[w]) with
- * correctly rounded IEEE operations and no contraction into fused
- * multiply-adds, so a CPU restatement of the same order reproduces every
- * bit.  bc accumulates the roots in the order given.
+ * All operations are correctly rounded IEEE double with no contraction into
+ * fused multiply-adds, so a CPU restatement of the same order reproduces
+ * every bit.  bc accumulates the roots in the order given.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -61,7 +63,7 @@ struct SweepParams {
   int levels;
   int root;                          /* caller numbering ...                 */
   const int *inv;                    /* ... mapped by inv (or null)          */
-  double *delta;                     /* n, zero on entry                     */
+  double *q;                         /* n: (1 + delta[v]) / sigma[v], zero on entry */
   double *bc;                        /* n, accumulated                       */
   /* hubs (out-degree > kSeg) by list position i: segoff[i] (exclusive prefix
    * of their segment counts over positions), hoff[i] (of the hub flags);
@@ -73,15 +75,18 @@ struct SweepParams {
   long long timeout_ns;
 };
 
-__device__ __forceinline__ double term(const SweepParams &p, double sv, int w) {
-  const double sw = (double)__ldg(p.sig + w);
-  return __dmul_rn(__ddiv_rn(sv, sw), __dadd_rn(1.0, __ldcg(p.delta + w)));
+/* v is final with the sum acc of its children's q: delta[v] to bc, q[v] */
+__device__ __forceinline__ void finish(const SweepParams &p, int v, int root, double acc) {
+  const double sv = (double)__ldg(p.sig + v);
+  const double dv = __dmul_rn(sv, acc);
+  p.q[v] = __ddiv_rn(__dadd_rn(1.0, dv), sv);
+  if (v != root) p.bc[v] = __dadd_rn(p.bc[v], dv);
 }
 
-/* acc += the terms of entries k0, k0 + step, ... < e, in that order; four
- * entries' loads are issued before their terms are added */
-__device__ __forceinline__ double sum_entries(const SweepParams &p, int d, double sv, int k0,
-                                              int e, int step) {
+/* acc += q[w] of the entries k0, k0 + step, ... < e with S[w] = d + 1, in
+ * that order; four entries' loads are issued before they are added */
+__device__ __forceinline__ double sum_entries(const SweepParams &p, int d, int k0, int e,
+                                              int step) {
   double acc = 0.0;
   int k = k0;
   for (; k + 3 * step < e; k += 4 * step) {
@@ -93,23 +98,23 @@ __device__ __forceinline__ double sum_entries(const SweepParams &p, int d, doubl
     for (int j = 0; j < 4; ++j) c[j] = __ldg(p.S + w[j]) == d + 1;
     double t[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) t[j] = c[j] ? term(p, sv, w[j]) : 0.0;
+    for (int j = 0; j < 4; ++j) t[j] = c[j] ? __ldcg(p.q + w[j]) : 0.0;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
       if (c[j]) acc = __dadd_rn(acc, t[j]);
   }
   for (; k < e; k += step) {
     const int w = __ldg(p.jr + k);
-    if (__ldg(p.S + w) == d + 1) acc = __dadd_rn(acc, term(p, sv, w));
+    if (__ldg(p.S + w) == d + 1) acc = __dadd_rn(acc, __ldcg(p.q + w));
   }
   return acc;
 }
 
 /* the terms of [b, e) summed lane-strided over the warp, then the butterfly;
  * every lane returns the same value (lane 0's order) */
-__device__ __forceinline__ double warp_sum(const SweepParams &p, int d, double sv, int b, int e) {
+__device__ __forceinline__ double warp_sum(const SweepParams &p, int d, int b, int e) {
   const int lane = threadIdx.x & 31;
-  double acc = sum_entries(p, d, sv, b + lane, e, 32);
+  double acc = sum_entries(p, d, b + lane, e, 32);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(FULL, acc, o));
   return __shfl_sync(FULL, acc, 0);
@@ -121,6 +126,14 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
   const unsigned gwarp = (blockIdx.x * kBlock + threadIdx.x) >> 5;
   const unsigned nwarps = (gridDim.x * kBlock) >> 5;
   const unsigned gthread = blockIdx.x * kBlock + threadIdx.x;
+  { /* the deepest level has no children: delta = 0, q = 1 / sigma */
+    const int lo = __ldg(p.off + p.levels - 1), hi = __ldg(p.off + p.levels);
+    for (int i = lo + (int)gthread; i < hi; i += (int)(gridDim.x * kBlock)) {
+      const int v = __ldg(p.list + i);
+      p.q[v] = __ddiv_rn(1.0, (double)__ldg(p.sig + v));
+    }
+    if (!grid_barrier(p.ctl, p.timeout_ns, p.levels - 1)) return;
+  }
   for (int d = p.levels - 2; d >= 0; --d) {
     const int lo = __ldg(p.off + d), hi = __ldg(p.off + d + 1);
     const int s_lo = __ldg(p.segoff + lo), s_hi = __ldg(p.segoff + hi);
@@ -138,11 +151,7 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
           e = __ldg(p.rp + v + 1);
         }
         const bool heavy = v >= 0 && e - b >= kWarpDegree && e - b <= kSeg;
-        if (v >= 0 && e - b < kWarpDegree) {
-          const double acc = sum_entries(p, d, (double)__ldg(p.sig + v), b, e, 1);
-          p.delta[v] = acc;
-          if (v != root) p.bc[v] = __dadd_rn(p.bc[v], acc);
-        }
+        if (v >= 0 && e - b < kWarpDegree) finish(p, v, root, sum_entries(p, d, b, e, 1));
         /* one-segment lists of the chunk, one at a time with the whole warp */
         unsigned hv = __ballot_sync(FULL, heavy);
         while (hv) {
@@ -150,11 +159,8 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
           hv &= hv - 1u;
           const int vv = __shfl_sync(FULL, v, src);
           const int bb = __shfl_sync(FULL, b, src), ee = __shfl_sync(FULL, e, src);
-          const double acc = warp_sum(p, d, (double)__ldg(p.sig + vv), bb, ee);
-          if (lane == 0) {
-            p.delta[vv] = acc;
-            if (vv != root) p.bc[vv] = __dadd_rn(p.bc[vv], acc);
-          }
+          const double acc = warp_sum(p, d, bb, ee);
+          if (lane == 0) finish(p, vv, root, acc);
         }
       } else { /* segment s of a hub */
         const int sg = s_lo + (int)(it - nch);
@@ -162,7 +168,7 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
         const int v = __ldg(p.list + i);
         const int b = __ldg(p.rp + v) + (sg - __ldg(p.segoff + i)) * kSeg;
         const int e = min(b + kSeg, __ldg(p.rp + v + 1));
-        const double acc = warp_sum(p, d, (double)__ldg(p.sig + v), b, e);
+        const double acc = warp_sum(p, d, b, e);
         if (lane == 0) p.part[sg] = acc;
       }
     }
@@ -174,8 +180,7 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
         const int s0 = __ldg(p.segoff + i), s1 = __ldg(p.segoff + i + 1);
         double acc = __ldcg(p.part + s0);
         for (int sg = s0 + 1; sg < s1; ++sg) acc = __dadd_rn(acc, __ldcg(p.part + sg));
-        p.delta[v] = acc;
-        if (v != root) p.bc[v] = __dadd_rn(p.bc[v], acc);
+        finish(p, v, root, acc);
       }
     }
     if (!grid_barrier(p.ctl, p.timeout_ns, d)) return;
@@ -433,7 +438,7 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
     p.levels = levels;
     p.root = roots[r];
     p.inv = g->inv;
-    p.delta = w.delta;
+    p.q = w.delta;
     p.bc = w.bc;
     p.segoff = w.segoff;
     p.hoff = w.hoff;
