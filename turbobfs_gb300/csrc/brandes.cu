@@ -188,21 +188,28 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
 }
 
 /* segs[i] = segments of the vertex at list position i (0 unless a hub),
- * flag[i] = it is a hub; i < cnt */
-__global__ void hub_count_kernel(const int *list, const int *rp, int cnt, int *segs, int *flag) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-    const int v = list[i];
-    const int deg = rp[v + 1] - rp[v];
-    const int h = deg > kSeg ? 1 : 0;
-    segs[i] = h ? (deg + kSeg - 1) / kSeg : 0;
+ * flag[i] = it is a hub; for i < *cnt (the reached vertices), 0 up to len */
+__global__ void hub_count_kernel(const int *list, const int *rp, const int *cnt, int len,
+                                 int *segs, int *flag) {
+  const int c = *cnt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+    int h = 0, sg = 0;
+    if (i < c) {
+      const int v = list[i];
+      const int deg = rp[v + 1] - rp[v];
+      h = deg > kSeg ? 1 : 0;
+      sg = h ? (deg + kSeg - 1) / kSeg : 0;
+    }
+    segs[i] = sg;
     flag[i] = h;
   }
 }
 
 /* hubpos[hoff[i]] = i and seg_hub[s] = hoff[i] for the hubs' segments */
-__global__ void hub_fill_kernel(const int *segoff, const int *hoff, int cnt, int *hubpos,
-                                int *seg_hub) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+__global__ void hub_fill_kernel(const int *segoff, const int *hoff, const int *cnt,
+                                int *hubpos, int *seg_hub) {
+  const int c = *cnt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c; i += gridDim.x * blockDim.x) {
     const int h = hoff[i];
     if (hoff[i + 1] == h) continue;
     hubpos[h] = i;
@@ -300,8 +307,8 @@ tbfs_status bfail(cudaError_t e, const char *what) {
 struct Scratch {
   int *S = nullptr, *list = nullptr, *off = nullptr, *fill = nullptr;
   int *segoff = nullptr, *hoff = nullptr, *hubpos = nullptr, *seg_hub = nullptr;
+  int *partial = nullptr; /* scan scratch */
   double *part = nullptr;
-  long long part_cap = 0;
   unsigned long long *sig = nullptr;
   double *delta = nullptr, *bc = nullptr, *out = nullptr;
   SweepCtl *ctl = nullptr;
@@ -317,6 +324,7 @@ struct Scratch {
     cudaFree(hubpos);
     cudaFree(seg_hub);
     cudaFree(part);
+    cudaFree(partial);
     cudaFree(sig);
     cudaFree(delta);
     cudaFree(bc);
@@ -355,6 +363,12 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
   BTRY(cudaMalloc(&w.segoff, (n + 1) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.hoff, (n + 1) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.hubpos, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.partial, (size_t)tbfs::scan_partials((long long)n + 2) * sizeof(int)),
+       "alloc");
+  /* segments: each hub has deg > kSeg, so sum of ceil(deg / kSeg) < 2 nnz / kSeg + 1 */
+  const size_t seg_cap = (size_t)(2 * g->nnz / tbfs::kSeg + 1);
+  BTRY(cudaMalloc(&w.part, seg_cap * sizeof(double)), "alloc");
+  BTRY(cudaMalloc(&w.seg_hub, seg_cap * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.delta, n * sizeof(double)), "alloc");
   BTRY(cudaMalloc(&w.bc, n * sizeof(double)), "alloc");
   BTRY(cudaMalloc(&w.ctl, sizeof(SweepCtl)), "alloc");
@@ -391,41 +405,24 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
     BTRY(cudaMemsetAsync(w.off, 0, ((size_t)levels + 1) * sizeof(int), s), "clear");
     tbfs::level_count_kernel<<<tiles, tbfs::kBlock, 0, s>>>(w.S, g->n, levels, w.off);
     BTRY(cudaGetLastError(), "level count");
-    BTRY(tbfs::exclusive_scan(w.off, (long long)levels + 1, w.off, s), "level prefix");
+    BTRY(tbfs::exclusive_scan_ws(w.off, (long long)levels + 1, w.off, w.partial, s),
+         "level prefix");
     BTRY(cudaMemcpyAsync(w.fill, w.off, (size_t)levels * sizeof(int), cudaMemcpyDeviceToDevice, s),
          "fill pointers");
     tbfs::level_fill_kernel<<<tiles, tbfs::kBlock, 0, s>>>(w.S, g->n, levels, w.fill, w.list);
     BTRY(cudaGetLastError(), "level fill");
-    /* hubs: segment counts and flags by list position, their prefixes, the
-     * hub and segment maps */
-    int reached = 0;
-    BTRY(cudaMemcpyAsync(&reached, w.off + levels, sizeof(int), cudaMemcpyDeviceToHost, s),
-         "reached");
-    BTRY(cudaStreamSynchronize(s), "reached");
-    const unsigned cgrid = (unsigned)((reached + 255) / 256 > 0 ? (reached + 255) / 256 : 1);
-    BTRY(cudaMemsetAsync(w.segoff + reached, 0, sizeof(int), s), "clear");
-    BTRY(cudaMemsetAsync(w.hoff + reached, 0, sizeof(int), s), "clear");
-    tbfs::hub_count_kernel<<<cgrid, 256, 0, s>>>(w.list, g->rp, reached, w.segoff, w.hoff);
+    /* hubs: segment counts and flags by list position (positions < off[levels],
+     * the reached vertices), their prefixes, the hub and segment maps */
+    const unsigned cgrid = (unsigned)((n + 1 + 255) / 256);
+    tbfs::hub_count_kernel<<<cgrid, 256, 0, s>>>(w.list, g->rp, w.off + levels, g->n + 1,
+                                                 w.segoff, w.hoff);
     BTRY(cudaGetLastError(), "hub count");
-    BTRY(tbfs::exclusive_scan(w.segoff, (long long)reached + 1, w.segoff, s), "segment prefix");
-    BTRY(tbfs::exclusive_scan(w.hoff, (long long)reached + 1, w.hoff, s), "hub prefix");
-    int nseg = 0;
-    BTRY(cudaMemcpyAsync(&nseg, w.segoff + reached, sizeof(int), cudaMemcpyDeviceToHost, s),
-         "segments");
-    BTRY(cudaStreamSynchronize(s), "segments");
-    if (nseg > w.part_cap) {
-      cudaFree(w.part);
-      cudaFree(w.seg_hub);
-      w.part = nullptr;
-      w.seg_hub = nullptr;
-      BTRY(cudaMalloc(&w.part, (size_t)nseg * sizeof(double)), "alloc");
-      BTRY(cudaMalloc(&w.seg_hub, (size_t)nseg * sizeof(int)), "alloc");
-      w.part_cap = nseg;
-    }
-    if (nseg > 0) {
-      tbfs::hub_fill_kernel<<<cgrid, 256, 0, s>>>(w.segoff, w.hoff, reached, w.hubpos, w.seg_hub);
-      BTRY(cudaGetLastError(), "hub fill");
-    }
+    BTRY(tbfs::exclusive_scan_ws(w.segoff, (long long)n + 1, w.segoff, w.partial, s),
+         "segment prefix");
+    BTRY(tbfs::exclusive_scan_ws(w.hoff, (long long)n + 1, w.hoff, w.partial, s), "hub prefix");
+    tbfs::hub_fill_kernel<<<cgrid, 256, 0, s>>>(w.segoff, w.hoff, w.off + levels, w.hubpos,
+                                                w.seg_hub);
+    BTRY(cudaGetLastError(), "hub fill");
     BTRY(cudaMemsetAsync(w.delta, 0, n * sizeof(double), s), "clear");
     BTRY(cudaMemsetAsync(w.ctl, 0, sizeof(SweepCtl), s), "clear");
     SweepParams p;

@@ -229,17 +229,28 @@ int grid_for(long long work) {
 
 }  // namespace
 
+long long scan_partials(long long len) { return (len + kScanTile - 1) / kScanTile; }
+
+/* exclusive scan over len ints with the caller's partial-sum scratch; queued
+ * on s, no synchronisation */
+cudaError_t exclusive_scan_ws(const int *in, long long len, int *out, int *partial,
+                              cudaStream_t s) {
+  const long long tiles = scan_partials(len);
+  if (tiles == 0) return cudaSuccess;
+  scan_reduce_kernel<<<(unsigned)tiles, kThreads, 0, s>>>(in, len, partial);
+  scan_partials_kernel<<<1, kThreads, 0, s>>>(partial, (int)tiles);
+  scan_apply_kernel<<<(unsigned)tiles, kThreads, 0, s>>>(in, len, partial, out);
+  return cudaGetLastError();
+}
+
 /* exclusive scan over len ints, in place allowed; synchronises the stream */
 cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t s) {
-  const long long tiles = (len + kScanTile - 1) / kScanTile;
+  const long long tiles = scan_partials(len);
   if (tiles == 0) return cudaSuccess;
   int *partial = nullptr;
   cudaError_t e = cudaMalloc(&partial, (size_t)tiles * sizeof(int));
   if (e != cudaSuccess) return e;
-  scan_reduce_kernel<<<(unsigned)tiles, kThreads, 0, s>>>(in, len, partial);
-  scan_partials_kernel<<<1, kThreads, 0, s>>>(partial, (int)tiles);
-  scan_apply_kernel<<<(unsigned)tiles, kThreads, 0, s>>>(in, len, partial, out);
-  e = cudaGetLastError();
+  e = exclusive_scan_ws(in, len, out, partial, s);
   cudaError_t e2 = cudaStreamSynchronize(s);
   cudaFree(partial);
   return e != cudaSuccess ? e : e2;

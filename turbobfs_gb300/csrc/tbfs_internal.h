@@ -251,6 +251,11 @@ cudaError_t mm_parse_device(const char *text, long long len, long long nz, long 
                             long long *bad_out, cudaStream_t s);
 /* exclusive prefix sum of len ints (in place allowed); synchronises s */
 cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t s);
+/* the same queued on s without synchronising, with the caller's scratch of
+ * scan_partials(len) ints */
+long long scan_partials(long long len);
+cudaError_t exclusive_scan_ws(const int *in, long long len, int *out, int *partial,
+                              cudaStream_t s);
 cudaError_t expand_columns(const int *cp, int n, int *col_of_entry, cudaStream_t s);
 /* Degree-based grouping of the vertices (see graph_ingest.cu).  On return
  * *identity tells whether the order is unchanged (then perm/inv/cp2/ic2 are
