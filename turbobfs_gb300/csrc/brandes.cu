@@ -50,7 +50,8 @@ constexpr int kSeg = 2048;        /* entries per segment of a hub's list        
 
 struct __align__(128) SweepCtl {
   int status, timeout_level;
-  int pad0[30];
+  unsigned work[4]; /* dynamic work counter of level d in work[d % 4] */
+  int pad0[26];
   GridBarrier bar;
 };
 
@@ -71,6 +72,9 @@ struct SweepParams {
    * part[s] = sum of segment s */
   const int *segoff, *hoff, *hubpos, *seg_hub;
   double *part;
+  /* vertices with 32 <= out-degree <= kSeg (a warp each): moff[i] exclusive
+   * prefix of their flags over positions, medpos[m] = position of the m-th */
+  const int *moff, *medpos;
   SweepCtl *ctl;
   long long timeout_ns;
 };
@@ -138,39 +142,41 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
     const int lo = __ldg(p.off + d), hi = __ldg(p.off + d + 1);
     const int s_lo = __ldg(p.segoff + lo), s_hi = __ldg(p.segoff + hi);
     const int h_lo = __ldg(p.hoff + lo), h_hi = __ldg(p.hoff + hi);
+    const int m_lo = __ldg(p.moff + lo), m_hi = __ldg(p.moff + hi);
+    const unsigned ns = (unsigned)(s_hi - s_lo), nm = (unsigned)(m_hi - m_lo);
     const unsigned nch = (unsigned)(hi - lo + 31) / 32u;
-    const unsigned items = nch + (unsigned)(s_hi - s_lo);
-    /* items: chunks of 32 vertices of level d, then the hubs' segments */
-    for (unsigned it = gwarp; it < items; it += nwarps) {
-      if (it < nch) {
-        const int i = lo + (int)it * 32 + lane;
-        int v = -1, b = 0, e = 0;
-        if (i < hi) {
-          v = __ldg(p.list + i);
-          b = __ldg(p.rp + v);
-          e = __ldg(p.rp + v + 1);
-        }
-        const bool heavy = v >= 0 && e - b >= kWarpDegree && e - b <= kSeg;
-        if (v >= 0 && e - b < kWarpDegree) finish(p, v, root, sum_entries(p, d, b, e, 1));
-        /* one-segment lists of the chunk, one at a time with the whole warp */
-        unsigned hv = __ballot_sync(FULL, heavy);
-        while (hv) {
-          const int src = __ffs(hv) - 1;
-          hv &= hv - 1u;
-          const int vv = __shfl_sync(FULL, v, src);
-          const int bb = __shfl_sync(FULL, b, src), ee = __shfl_sync(FULL, e, src);
-          const double acc = warp_sum(p, d, bb, ee);
-          if (lane == 0) finish(p, vv, root, acc);
-        }
-      } else { /* segment s of a hub */
-        const int sg = s_lo + (int)(it - nch);
+    const unsigned items = ns + nm + nch;
+    /* work counter of level d-2 (last used at level d+2) */
+    if (gthread == 0) p.ctl->work[(d + 2) & 3] = 0u;
+    /* items, the long ones first: the hubs' segments, then the vertices a
+     * warp sums, then chunks of 32 positions whose short lists one lane
+     * each sums.  The first item of a warp is static, the rest claimed. */
+    unsigned it = gwarp;
+    while (it < items) {
+      if (it < ns) { /* segment sg of a hub */
+        const int sg = s_lo + (int)it;
         const int i = __ldg(p.hubpos + __ldg(p.seg_hub + sg));
         const int v = __ldg(p.list + i);
         const int b = __ldg(p.rp + v) + (sg - __ldg(p.segoff + i)) * kSeg;
         const int e = min(b + kSeg, __ldg(p.rp + v + 1));
         const double acc = warp_sum(p, d, b, e);
         if (lane == 0) p.part[sg] = acc;
+      } else if (it < ns + nm) { /* a one-segment list, the whole warp */
+        const int v = __ldg(p.list + __ldg(p.medpos + m_lo + (int)(it - ns)));
+        const double acc = warp_sum(p, d, __ldg(p.rp + v), __ldg(p.rp + v + 1));
+        if (lane == 0) finish(p, v, root, acc);
+      } else { /* short lists, one lane each */
+        const int i = lo + (int)(it - ns - nm) * 32 + lane;
+        if (i < hi) {
+          const int v = __ldg(p.list + i);
+          const int b = __ldg(p.rp + v), e = __ldg(p.rp + v + 1);
+          if (e - b < kWarpDegree) finish(p, v, root, sum_entries(p, d, b, e, 1));
+        }
       }
+      if (items <= nwarps) break;
+      unsigned nxt = 0;
+      if (lane == 0) nxt = nwarps + atomicAdd(&p.ctl->work[d & 3], 1u);
+      it = __shfl_sync(FULL, nxt, 0);
     }
     if (h_hi > h_lo) { /* the hubs of level d: their segments in order */
       if (!grid_barrier(p.ctl, p.timeout_ns, d)) return;
@@ -188,21 +194,31 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepParams p) {
 }
 
 /* segs[i] = segments of the vertex at list position i (0 unless a hub),
- * flag[i] = it is a hub; for i < *cnt (the reached vertices), 0 up to len */
+ * flag[i] = it is a hub, mflag[i] = a warp sums its list; for i < *cnt (the
+ * reached vertices), 0 up to len */
 __global__ void hub_count_kernel(const int *list, const int *rp, const int *cnt, int len,
-                                 int *segs, int *flag) {
+                                 int *segs, int *flag, int *mflag) {
   const int c = *cnt;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
-    int h = 0, sg = 0;
+    int h = 0, sg = 0, m = 0;
     if (i < c) {
       const int v = list[i];
       const int deg = rp[v + 1] - rp[v];
       h = deg > kSeg ? 1 : 0;
       sg = h ? (deg + kSeg - 1) / kSeg : 0;
+      m = deg >= kWarpDegree && deg <= kSeg ? 1 : 0;
     }
     segs[i] = sg;
     flag[i] = h;
+    mflag[i] = m;
   }
+}
+
+/* medpos[moff[i]] = i for the positions a warp sums */
+__global__ void med_fill_kernel(const int *moff, const int *cnt, int *medpos) {
+  const int c = *cnt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c; i += gridDim.x * blockDim.x)
+    if (moff[i + 1] != moff[i]) medpos[moff[i]] = i;
 }
 
 /* hubpos[hoff[i]] = i and seg_hub[s] = hoff[i] for the hubs' segments */
@@ -307,6 +323,7 @@ tbfs_status bfail(cudaError_t e, const char *what) {
 struct Scratch {
   int *S = nullptr, *list = nullptr, *off = nullptr, *fill = nullptr;
   int *segoff = nullptr, *hoff = nullptr, *hubpos = nullptr, *seg_hub = nullptr;
+  int *moff = nullptr, *medpos = nullptr;
   int *partial = nullptr; /* scan scratch */
   double *part = nullptr;
   unsigned long long *sig = nullptr;
@@ -323,6 +340,8 @@ struct Scratch {
     cudaFree(hoff);
     cudaFree(hubpos);
     cudaFree(seg_hub);
+    cudaFree(moff);
+    cudaFree(medpos);
     cudaFree(part);
     cudaFree(partial);
     cudaFree(sig);
@@ -363,6 +382,8 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
   BTRY(cudaMalloc(&w.segoff, (n + 1) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.hoff, (n + 1) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.hubpos, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.moff, (n + 1) * sizeof(int)), "alloc");
+  BTRY(cudaMalloc(&w.medpos, (n + 1) * sizeof(int)), "alloc");
   BTRY(cudaMalloc(&w.partial, (size_t)tbfs::scan_partials((long long)n + 2) * sizeof(int)),
        "alloc");
   /* segments: each hub has deg > kSeg, so sum of ceil(deg / kSeg) < 2 nnz / kSeg + 1 */
@@ -415,11 +436,14 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
      * the reached vertices), their prefixes, the hub and segment maps */
     const unsigned cgrid = (unsigned)((n + 1 + 255) / 256);
     tbfs::hub_count_kernel<<<cgrid, 256, 0, s>>>(w.list, g->rp, w.off + levels, g->n + 1,
-                                                 w.segoff, w.hoff);
+                                                 w.segoff, w.hoff, w.moff);
     BTRY(cudaGetLastError(), "hub count");
     BTRY(tbfs::exclusive_scan_ws(w.segoff, (long long)n + 1, w.segoff, w.partial, s),
          "segment prefix");
     BTRY(tbfs::exclusive_scan_ws(w.hoff, (long long)n + 1, w.hoff, w.partial, s), "hub prefix");
+    BTRY(tbfs::exclusive_scan_ws(w.moff, (long long)n + 1, w.moff, w.partial, s), "warp prefix");
+    tbfs::med_fill_kernel<<<cgrid, 256, 0, s>>>(w.moff, w.off + levels, w.medpos);
+    BTRY(cudaGetLastError(), "warp positions");
     tbfs::hub_fill_kernel<<<cgrid, 256, 0, s>>>(w.segoff, w.hoff, w.off + levels, w.hubpos,
                                                 w.seg_hub);
     BTRY(cudaGetLastError(), "hub fill");
@@ -441,6 +465,8 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
     p.hoff = w.hoff;
     p.hubpos = w.hubpos;
     p.seg_hub = w.seg_hub;
+    p.moff = w.moff;
+    p.medpos = w.medpos;
     p.part = w.part;
     p.ctl = w.ctl;
     p.timeout_ns = timeout;
