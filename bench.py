@@ -59,12 +59,15 @@ def parse_args():
     p.add_argument("--cpu-threads", type=int, default=0)
     p.add_argument("--no-autotune", action="store_true",
                    help="default alpha/beta/pull_ratio instead of the autotuned ones")
-    p.add_argument("--part", choices=["all", "batched", "serving", "ingest", "brandes"],
+    p.add_argument("--part", choices=["all", "batched", "serving", "ingest", "brandes",
+                                      "directed"],
                    default="all", help="run only that report and print it")
     p.add_argument("--no-batched", action="store_true", help="skip the batched report")
     p.add_argument("--no-serving", action="store_true", help="skip the serving report")
     p.add_argument("--no-ingest", action="store_true", help="skip the ingest report")
     p.add_argument("--ingest-scale", type=int, default=21)
+    p.add_argument("--no-directed", action="store_true", help="skip the directed-graph report")
+    p.add_argument("--directed-scale", type=int, default=22)
     p.add_argument("--no-brandes", action="store_true", help="skip the betweenness report")
     p.add_argument("--brandes-scale", type=int, default=20)
     p.add_argument("--brandes-roots", type=int, default=16)
@@ -372,6 +375,8 @@ def run_tbfs(args, world, rank, local):
         line["ingest"] = ingest_report(args)
     if rank == 0 and world == 1 and not args.no_brandes:
         line["brandes"] = brandes_report(args)
+    if rank == 0 and world == 1 and not args.no_directed:
+        line["directed"] = directed_report(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
@@ -830,6 +835,56 @@ def brandes_report(args):
                            "host wall clock around tbfs_brandes"}
 
 
+def directed_report(args):
+    """Directed graph: every undirected RMAT edge kept in one direction (a
+    hash of the pair picks which), uploaded without TBFS_GRAPH_SYMMETRIC so
+    the out-lists are built on the device.  Direction-optimizing BFS (pushes
+    over out-lists, pulls over in-lists) against pulls only (mode bu, the
+    structure of the reference's column-per-thread kernels), S + sigma, with
+    two roots checked against the oracle."""
+    import oracle
+    import turbobfs_gb300 as tb
+    from turbobfs_gb300 import graphs
+
+    scale = args.directed_scale
+    hs = graphs.rmat(scale, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    col = np.repeat(np.arange(hs.n, dtype=np.int64), np.diff(hs.col_ptr))
+    row = hs.row_idx.astype(np.int64)
+    pick = (((row ^ col) * 0x9E3779B1) >> 16) & 1
+    keep = pick == (row < col)
+    h = graphs.from_edges(hs.n, row[keep].astype(np.int32), col[keep].astype(np.int32))
+    del hs, col, row
+    deg_in = np.diff(h.col_ptr)
+    rng = np.random.default_rng(4)
+    cand = np.nonzero(deg_in > 0)[0]
+    roots = cand[rng.integers(0, cand.shape[0], 16)].astype(np.int32)
+    out = {"workload": f"RMAT scale {scale}, edgefactor 16, each undirected edge kept in one "
+                       "direction; 16 roots with in-edges; S + sigma",
+           "n": int(h.n), "nnz": int(h.nnz)}
+    t0 = time.perf_counter()
+    with tb.Graph.from_host_csc(h) as g:  # not symmetric: device transpose
+        out["upload_with_transpose_ms"] = (time.perf_counter() - t0) * 1e3
+        for mode in ("auto", "bu"):
+            for r in roots[:2]:
+                g.bfs(int(r), mode=mode)
+            ms, edges = [], []
+            for r in roots:
+                res = g.bfs(int(r), mode=mode)
+                ms.append(res.stats["device_ms"])
+                edges.append(res.stats["edges"])
+            out[f"{mode}_ms_per_bfs"] = float(np.mean(ms))
+            out[f"{mode}_gteps"] = float(np.sum(edges) / (np.sum(ms) * 1e-3) / 1e9)
+        same = True
+        for r in roots[:2]:
+            res = g.bfs(int(r))
+            S, sg, ovf, _ = oracle.exact_bfs(h.col_ptr, h.row_idx, int(r))
+            same &= bool(np.array_equal(res.S, S) and np.array_equal(res.sigma[ovf == 0], sg[ovf == 0]))
+    out["push_pull_speedup_vs_pull_only"] = out["bu_ms_per_bfs"] / out["auto_ms_per_bfs"]
+    out["identical_to_oracle"] = same
+    out["gteps_edges"] = "out-list entries of the root's reached vertices (stats.edges)"
+    return out
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_env()
@@ -840,7 +895,8 @@ def main():
 
         torch.cuda.set_device(local)
         rep = {"batched": batched_report, "serving": serving_report,
-               "ingest": ingest_report, "brandes": brandes_report}[args.part](args)
+               "ingest": ingest_report, "brandes": brandes_report,
+               "directed": directed_report}[args.part](args)
         print(json.dumps({"part": args.part, args.part: rep}), flush=True)
         return 0
     return run_tbfs(args, world, rank, local)
