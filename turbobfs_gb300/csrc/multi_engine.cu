@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
     /* rounds per item: enough items for every warp on small levels */
     s_part[t] = (unsigned)min(esum, 0xffffffffull);
     if (act) s_active = 1;
-    if (fin && P.stop_on_done) ctl->stop = 1; /* CTA 0 only; read after the barrier */
+    if (fin && P.stop_on_done) ctl->stop[ph & 1u] = 1; /* CTA 0 only; read after the barrier */
     __syncthreads();
     for (int o = kBlock / 2; o > 0; o >>= 1) {
       if (t < o) s_part[t] = (unsigned)min((unsigned long long)s_part[t] + s_part[t + o],
@@ -309,12 +309,12 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
       it = __shfl_sync(FULL, nx, 0);
     }
     /* a waiting request (host flag) ends the launch after this level */
-    if (tid == 0 && P.wake && *P.wake) ctl->stop = 1;
+    if (tid == 0 && P.wake && *P.wake) ctl->stop[ph & 1u] = 1;
     if (!grid_barrier(ctl, P.timeout_ns, (int)ph)) return;
     for (int i = t; i < ns; i += kBlock)
       if (s_qn[i]) s_d[i] += 1;
     __syncthreads();
-    if (__ldcg(&ctl->stop)) {
+    if (__ldcg(&ctl->stop[ph & 1u])) {
       ++ph;
       break;
     }

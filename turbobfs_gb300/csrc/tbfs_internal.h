@@ -196,8 +196,11 @@ struct __align__(128) MultiCtl {
   unsigned work[4];
   int status, timeout_level;
   int phases;                 /* levels run by the launch */
-  int stop;                   /* end the launch after the current level */
-  int pad0[24];
+  int stop[2];                /* end the launch after level ph: stop[ph % 2], written
+                                 during the level, read after its barrier; two slots
+                                 so that a CTA already in level ph+1 cannot write
+                                 the word a slower CTA is still to read for ph */
+  int pad0[23];
   GridBarrier bar;
 };
 
