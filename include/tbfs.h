@@ -142,6 +142,11 @@ tbfs_status tbfs_graph_load_mm(const char *path, int32_t undirected, uint32_t bu
  * with TBFS_GRAPH_KEEP_ORDER to read it back). */
 tbfs_status tbfs_graph_get_csc(const tbfs_graph *g, int32_t *col_ptr, int32_t *row_idx);
 
+/* The same lists as COOC pairs row[k] -> col[k] (nnz each, in column order:
+ * the reference's ICOOC / JCOOC, TurboBFS_COOC_TD/bfstdcooc.h:29-32), the
+ * column of every entry expanded on the device. */
+tbfs_status tbfs_graph_get_cooc(const tbfs_graph *g, int32_t *row, int32_t *col);
+
 void tbfs_graph_destroy(tbfs_graph *g);
 
 tbfs_status tbfs_graph_info(const tbfs_graph *g, int32_t *n, int64_t *nnz,

@@ -157,3 +157,19 @@ def test_cooc_lists_keep_file_order(gpu_available):
     with tb.Graph.from_cooc(I, J, n, keep_order=True) as g:
         cp, ic = g.csc()
     assert np.array_equal(cp, want.col_ptr) and np.array_equal(ic, want.row_idx)
+
+
+def test_mm_text_to_cooc(gpu_available):
+    """Matrix Market -> symmetric sorted COOC on the device: the column-order
+    pairs of the deduplicated symmetric CSC."""
+    n, m = 3000, 15000
+    rng = np.random.default_rng(12)
+    src = rng.integers(0, n, m, dtype=np.int32)
+    dst = rng.integers(0, n, m, dtype=np.int32)
+    text = _mm_text(n, src, dst, noise=False)
+    flags = BUILD_DROP_LOOPS | BUILD_DEDUP
+    want = graphs.from_edges(n, src, dst, symmetrize=True, drop_loops=True, dedup=True)
+    with tb.Graph.from_mm_text(text, True, flags, keep_order=True) as g:
+        row, col = g.cooc()
+    assert np.array_equal(row, want.row_idx)
+    assert np.array_equal(col, np.repeat(np.arange(n, dtype=np.int32), np.diff(want.col_ptr)))

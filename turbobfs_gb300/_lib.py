@@ -98,6 +98,7 @@ _SIGNATURES = {
                                      POINTER(c_void_p)]),
     "tbfs_graph_load_mm": (c_int, [c_char_p, c_int32, c_uint32, c_uint32, POINTER(c_void_p)]),
     "tbfs_graph_get_csc": (c_int, [c_void_p, _P_I32, _P_I32]),
+    "tbfs_graph_get_cooc": (c_int, [c_void_p, _P_I32, _P_I32]),
     "tbfs_autotune": (c_int, [c_void_p, _P_I32, c_int32, c_char_p, POINTER(Options),
                               POINTER(c_int32)]),
     "tbfs_brandes": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_void_p,

@@ -177,6 +177,15 @@ class Graph:
               "tbfs_graph_get_csc")
         return cp, ic[: self.nnz]
 
+    def cooc(self):
+        """The resident in-lists as COOC pairs (row, col), column order
+        (graphs created with keep_order=True)."""
+        row = np.empty(max(self.nnz, 1), np.int32)
+        col = np.empty(max(self.nnz, 1), np.int32)
+        check(lib().tbfs_graph_get_cooc(self.handle, _ptr(row, _P_I32), _ptr(col, _P_I32)),
+              "tbfs_graph_get_cooc")
+        return row[: self.nnz], col[: self.nnz]
+
     @property
     def handle(self) -> ctypes.c_void_p:
         if self._h is None:

@@ -535,6 +535,29 @@ extern "C" tbfs_status tbfs_graph_load_mm(const char *path, int32_t undirected,
   return st;
 }
 
+/* The resident in-lists as COOC pairs (row[k] -> col[k], entries in column
+ * order, the reference's ICOOC/JCOOC): rows copied, columns expanded on the
+ * device.  Same numbering rule as tbfs_graph_get_csc. */
+extern "C" tbfs_status tbfs_graph_get_cooc(const tbfs_graph *g, int32_t *row, int32_t *col) {
+  if (!g || (g->nnz > 0 && (!row || !col))) return invalid("tbfs_graph_get_cooc: null argument");
+  if (g->inv) {
+    tbfs_set_error("tbfs_graph_get_cooc: the graph is stored regrouped by degree");
+    return TBFS_ERR_UNSUPPORTED;
+  }
+  if (g->nnz == 0) return TBFS_OK;
+  CUDA_TRY(cudaSetDevice(g->device));
+  int *dcol = nullptr;
+  CUDA_TRY(cudaMalloc(&dcol, (size_t)g->nnz * sizeof(int)));
+  cudaError_t e = tbfs::expand_columns(g->cp, g->n, dcol, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(col, dcol, (size_t)g->nnz * sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(row, g->ic, (size_t)g->nnz * sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(dcol);
+  if (e != cudaSuccess) return cuda_fail(e, "tbfs_graph_get_cooc", __LINE__);
+  return TBFS_OK;
+}
+
 /* The resident in-lists back in the caller's numbering: only for graphs
  * kept in that numbering (TBFS_GRAPH_KEEP_ORDER, or a grouping that left the
  * order unchanged). */
