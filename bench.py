@@ -284,10 +284,10 @@ def run_tbfs(args, world, rank, local):
     tuning = {"autotuned": False}
     kw = {}
     if not args.no_autotune and args.mode == "auto":
-        # the library's autotuner, timed on 4 of the roots (not cached)
-        tu = g.autotune(roots[:4])
+        # the library's autotuner, timed on 8 of the roots (not cached)
+        tu = g.autotune(roots[:8])
         kw = {"alpha": tu["alpha"], "beta": tu["beta"], "pull_ratio": tu["pull_ratio"]}
-        tuning = {"autotuned": True, "sample_roots": 4, **kw}
+        tuning = {"autotuned": True, "sample_roots": 8, **kw}
     o = make_options(args.mode, True, outputs_on_device=True, **kw)
     stats = (_lib.Stats * k)()
     roots_c = np.ascontiguousarray(roots, dtype=np.int32)

@@ -35,9 +35,9 @@ def test_autotune_candidates_cache_and_results(gpu_available, tmp_path):
     with tb.Graph.from_host_csc(h) as g:
         t1 = g.autotune(roots, cache=cache)
         assert not t1["from_cache"]
-        assert t1["alpha"] in (2.0, 5.0, 15.0, 40.0, 120.0)
-        assert t1["beta"] in (2.0, 6.0, 18.0, 54.0, 162.0)
-        assert t1["pull_ratio"] in (0.25, 1.0, 4.0, 16.0)
+        assert t1["alpha"] in (4.0, 6.0, 9.0, 12.0, 15.0, 24.0, 60.0)
+        assert t1["beta"] in (1.0, 2.0, 4.0, 18.0)
+        assert t1["pull_ratio"] in (0.5, 1.0, 2.0, 4.0)
         t2 = g.autotune(roots, cache=cache)
         assert t2["from_cache"] and (t2["alpha"], t2["beta"], t2["pull_ratio"]) == \
             (t1["alpha"], t1["beta"], t1["pull_ratio"])

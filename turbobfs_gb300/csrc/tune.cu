@@ -9,8 +9,8 @@
  *
  * Autotuner: the direction switch (alpha, beta) and the path-count schedule
  * (pull_ratio) of the single-source engine are chosen by timing traversals
- * from sample roots (CUDA events), one parameter at a time over a short
- * candidate list, starting from the defaults.  The winner is cached under a
+ * from sample roots (CUDA events) for every combination of a small grid of
+ * candidates (and the defaults).  The winner is cached under a
  * key made of the profile's shape (log2 of n, nnz and the maximum degree,
  * and every histogram bucket rounded to a power of two): graphs of one
  * family and scale share it, so a later call returns without timing.
@@ -186,32 +186,26 @@ extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_
     *ms = best;
     return TBFS_OK;
   };
+  /* every combination of a grid around the values that win on RMAT-like and
+   * mesh-like graphs (coordinate search stalled in a local optimum there) */
   double cur = 0.0;
   st = time_of(a, b, pr, &cur);
-  const float alphas[] = {2.0f, 5.0f, 15.0f, 40.0f, 120.0f};
-  const float betas[] = {2.0f, 6.0f, 18.0f, 54.0f, 162.0f};
-  const float ratios[] = {0.25f, 1.0f, 4.0f, 16.0f};
-  for (float x : alphas) {
-    double t = 0.0;
-    if (st == TBFS_OK && x != a && (st = time_of(x, b, pr, &t)) == TBFS_OK && t < cur) {
-      cur = t;
-      a = x;
-    }
-  }
-  for (float x : betas) {
-    double t = 0.0;
-    if (st == TBFS_OK && x != b && (st = time_of(a, x, pr, &t)) == TBFS_OK && t < cur) {
-      cur = t;
-      b = x;
-    }
-  }
-  for (float x : ratios) {
-    double t = 0.0;
-    if (st == TBFS_OK && x != pr && (st = time_of(a, b, x, &t)) == TBFS_OK && t < cur) {
-      cur = t;
-      pr = x;
-    }
-  }
+  const float alphas[] = {4.0f, 6.0f, 9.0f, 12.0f, 15.0f, 24.0f, 60.0f};
+  const float betas[] = {1.0f, 2.0f, 4.0f, 18.0f};
+  const float ratios[] = {0.5f, 1.0f, 2.0f, 4.0f};
+  const float a0 = a, b0 = b, p0 = pr;
+  for (float xa : alphas)
+    for (float xb : betas)
+      for (float xp : ratios) {
+        double t = 0.0;
+        if (st != TBFS_OK || (xa == a0 && xb == b0 && xp == p0)) continue;
+        if ((st = time_of(xa, xb, xp, &t)) == TBFS_OK && t < cur) {
+          cur = t;
+          a = xa;
+          b = xb;
+          pr = xp;
+        }
+      }
   cudaFree(S);
   cudaFree(sg);
   if (st != TBFS_OK) return st;
