@@ -236,7 +236,10 @@ def run_reference(args, world, rank):
           "sample": f"each step: {len(sample)} of the {len(roots)} roots, one single-threaded "
                     f"BFS per core at a time ({lscpu_model()})",
           "algorithm": "restatement of TurboBFS_CSC_TDBU/bfstdcsc_seq.c (int sigma)"}
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+    # n_gpus: the N this arm was launched for, so the two arms' lines pair up;
+    # the reference path itself runs on host cores only (cpu_baseline.cores)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": max(world, args.gpus),
+            "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
             "data": "synthetic (seeded RMAT generator)", "impl": "reference",
