@@ -82,9 +82,17 @@ __global__ void keep_kernel(const unsigned *key, const unsigned *val, long long 
   }
 }
 
+/* cnt[key] += kept pairs; the keys are sorted, so a warp's lanes mostly
+ * share one: one atomic per distinct key of the warp (match_any) */
 __global__ void column_count_kernel(const unsigned *key, const int *keep, long long len, int *cnt) {
-  for (unsigned long long i = gtid(); i < (unsigned long long)len; i += gstride())
-    if (keep[i]) atomicAdd(cnt + key[i], 1);
+  const int lane = threadIdx.x & 31;
+  for (unsigned long long i = gtid(); i < (unsigned long long)len; i += gstride()) {
+    const unsigned act = __activemask();
+    const unsigned k = keep[i] ? key[i] : 0xffffffffu;
+    const unsigned peers = __match_any_sync(act, k);
+    if (k != 0xffffffffu && (peers & ((1u << lane) - 1u)) == 0u)
+      atomicAdd(cnt + k, __popc(peers));
+  }
 }
 
 /* rows of the kept pairs at their compacted positions (keep scanned) */
