@@ -300,6 +300,11 @@ tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t *d_row_idx,
                              int32_t *d_S, int64_t *d_sigma, void *stream,
                              tbfs_stats *stats);
 
+/* Device memory the library freed stays mapped in its pool (up to
+ * TBFS_POOL_KEEP_MB, default 8192 MB, per GPU) for the next graph or
+ * workspace; this hands all of it back to the driver now. */
+tbfs_status tbfs_release_cached_memory(void);
+
 /* Page-locked host buffers for fast host<->device copies. */
 tbfs_status tbfs_host_alloc_pinned(size_t bytes, void **ptr);
 void tbfs_host_free_pinned(void *ptr);

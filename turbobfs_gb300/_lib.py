@@ -118,6 +118,7 @@ _SIGNATURES = {
     "tbfs_bfs_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64,
                                  c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                                  POINTER(Stats)]),
+    "tbfs_release_cached_memory": (c_int, []),
     "tbfs_host_alloc_pinned": (c_int, [c_size_t, POINTER(c_void_p)]),
     "tbfs_host_free_pinned": (None, [c_void_p]),
     "tbfs_status_string": (c_char_p, [c_int]),

@@ -487,3 +487,9 @@ COMPAT_FUNCTIONS = {
 
 def device_count() -> int:
     return int(lib().tbfs_device_count())
+
+
+def release_cached_memory() -> None:
+    """Hand the device memory the library's pool keeps after frees back to
+    the driver (tbfs_release_cached_memory)."""
+    check(lib().tbfs_release_cached_memory(), "tbfs_release_cached_memory")

@@ -102,27 +102,31 @@ static void graph_free(tbfs_graph *g) {
   cudaGetDevice(&cur);
   cudaSetDevice(g->device);
   if (g->separate_out) {
-    cudaFree(g->rp);
-    cudaFree(g->jr);
+    tbfs::dev_free(g->rp);
+    tbfs::dev_free(g->jr);
   }
-  cudaFree(g->cp);
-  cudaFree(g->ic);
-  cudaFree(g->queues);
-  cudaFree(g->bitmaps);
-  cudaFree(g->inv);
-  cudaFree(g->perm);
-  cudaFree(g->S_work);
-  cudaFree(g->sigma_work);
-  cudaFree(g->ctl);
-  cudaFree(g->S_dev);
-  cudaFree(g->sigma_dev);
-  cudaFree(g->S_dev2);
-  cudaFree(g->sigma_dev2);
+  tbfs::dev_free(g->cp);
+  tbfs::dev_free(g->ic);
+  tbfs::dev_free(g->queues);
+  tbfs::dev_free(g->bitmaps);
+  tbfs::dev_free(g->inv);
+  tbfs::dev_free(g->perm);
+  tbfs::dev_free(g->S_work);
+  tbfs::dev_free(g->sigma_work);
+  tbfs::dev_free(g->ctl);
+  tbfs::dev_free(g->S_dev);
+  tbfs::dev_free(g->sigma_dev);
+  tbfs::dev_free(g->S_dev2);
+  tbfs::dev_free(g->sigma_dev2);
   if (g->copy_stream) cudaStreamDestroy(g->copy_stream);
-  cudaFree(g->trace_dev);
+  tbfs::dev_free(g->trace_dev);
   if (g->ctl_host) cudaFreeHost(g->ctl_host);
   if (g->ev0) cudaEventDestroy(g->ev0);
   if (g->ev1) cudaEventDestroy(g->ev1);
+  tbfs::dev_free(g->many_ctl);
+  if (g->many_ctl_host) cudaFreeHost(g->many_ctl_host);
+  for (auto x : g->many_ev) cudaEventDestroy(x);
+  for (auto x : g->many_sync) cudaEventDestroy(x);
   tbfs::batch_ws_free(g->batch);
   cudaSetDevice(cur);
   delete g;
@@ -144,13 +148,13 @@ static tbfs_status need_device() {
 /* allocations shared by both constructors, after cp/ic/rp/jr are set */
 static tbfs_status graph_finish(tbfs_graph *g) {
   const size_t n = (size_t)g->n;
-  CUDA_TRY(cudaMalloc(&g->queues, 9 * n * sizeof(int)));
-  CUDA_TRY(cudaMalloc(&g->bitmaps, 4 * ((n + 31) / 32) * sizeof(unsigned)));
+  CUDA_TRY(tbfs::dev_alloc(&g->queues, 9 * n * sizeof(int)));
+  CUDA_TRY(tbfs::dev_alloc(&g->bitmaps, 4 * ((n + 31) / 32) * sizeof(unsigned)));
   if (g->inv) {
-    CUDA_TRY(cudaMalloc(&g->S_work, n * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&g->sigma_work, n * sizeof(unsigned long long)));
+    CUDA_TRY(tbfs::dev_alloc(&g->S_work, n * sizeof(int)));
+    CUDA_TRY(tbfs::dev_alloc(&g->sigma_work, n * sizeof(unsigned long long)));
   }
-  CUDA_TRY(cudaMalloc(&g->ctl, sizeof(BfsCtl)));
+  CUDA_TRY(tbfs::dev_alloc(&g->ctl, sizeof(BfsCtl)));
   CUDA_TRY(cudaMallocHost(&g->ctl_host, sizeof(BfsCtl)));
   memset(g->ctl_host, 0, sizeof(BfsCtl));
   CUDA_TRY(cudaEventCreate(&g->ev0));
@@ -171,8 +175,8 @@ static tbfs_status build_csc(tbfs_graph *g, const int32_t *col_ptr, const int32_
   const size_t n = (size_t)g->n, nnz = (size_t)g->nnz;
   const cudaMemcpyKind kind = (g->flags & TBFS_GRAPH_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice
                                                                   : cudaMemcpyHostToDevice;
-  CUDA_TRY(cudaMalloc(&g->cp, (n + 1) * sizeof(int)));
-  CUDA_TRY(cudaMalloc(&g->ic, (nnz ? nnz : 1) * sizeof(int)));
+  CUDA_TRY(tbfs::dev_alloc(&g->cp, (n + 1) * sizeof(int)));
+  CUDA_TRY(tbfs::dev_alloc(&g->ic, (nnz ? nnz : 1) * sizeof(int)));
   CUDA_TRY(cudaMemcpy(g->cp, col_ptr, (n + 1) * sizeof(int), kind));
   if (nnz) CUDA_TRY(cudaMemcpy(g->ic, row_idx, nnz * sizeof(int), kind));
   CUDA_TRY(cudaMemset(d_flag, 0, sizeof(int)));
@@ -193,22 +197,22 @@ static tbfs_status finish_lists(tbfs_graph *g, int *d_flag) {
   if (!(g->flags & TBFS_GRAPH_KEEP_ORDER) && nnz > 0) {
     int *perm = nullptr, *inv = nullptr, *cp2 = nullptr, *ic2 = nullptr;
     bool identity = true;
-    cudaError_t e = cudaMalloc(&perm, n * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&inv, n * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&cp2, (n + 1) * sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&ic2, nnz * sizeof(int));
+    cudaError_t e = tbfs::dev_alloc(&perm, n * sizeof(int));
+    if (e == cudaSuccess) e = tbfs::dev_alloc(&inv, n * sizeof(int));
+    if (e == cudaSuccess) e = tbfs::dev_alloc(&cp2, (n + 1) * sizeof(int));
+    if (e == cudaSuccess) e = tbfs::dev_alloc(&ic2, nnz * sizeof(int));
     if (e == cudaSuccess)
       e = tbfs::degree_group_relabel(g->cp, g->ic, g->n, g->nnz, perm, inv, cp2, ic2, &identity,
                                      0);
     if (e != cudaSuccess || identity) {
-      cudaFree(perm);
-      cudaFree(inv);
-      cudaFree(cp2);
-      cudaFree(ic2);
+      tbfs::dev_free(perm);
+      tbfs::dev_free(inv);
+      tbfs::dev_free(cp2);
+      tbfs::dev_free(ic2);
       if (e != cudaSuccess) return cuda_fail(e, "degree grouping", __LINE__);
     } else {
-      cudaFree(g->cp);
-      cudaFree(g->ic);
+      tbfs::dev_free(g->cp);
+      tbfs::dev_free(g->ic);
       g->cp = cp2;
       g->ic = ic2;
       g->inv = inv;
@@ -222,14 +226,14 @@ static tbfs_status finish_lists(tbfs_graph *g, int *d_flag) {
   }
   /* out-lists = transpose: key = row id, value = column id */
   int *col = nullptr;
-  CUDA_TRY(cudaMalloc(&col, (nnz ? nnz : 1) * sizeof(int)));
+  CUDA_TRY(tbfs::dev_alloc(&col, (nnz ? nnz : 1) * sizeof(int)));
   g->separate_out = true;
-  cudaError_t e = cudaMalloc(&g->rp, (n + 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&g->jr, (nnz ? nnz : 1) * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&g->rp, (n + 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&g->jr, (nnz ? nnz : 1) * sizeof(int));
   if (e == cudaSuccess) e = tbfs::expand_columns(g->cp, g->n, col, 0);
   if (e == cudaSuccess)
     e = tbfs::counting_sort_lists(g->ic, col, g->nnz, g->n, g->rp, g->jr, d_flag, 0);
-  cudaFree(col);
+  tbfs::dev_free(col);
   if (e != cudaSuccess) return cuda_fail(e, "transpose", __LINE__);
   return TBFS_OK;
 }
@@ -249,14 +253,14 @@ extern "C" tbfs_status tbfs_graph_create_csc(const int32_t *col_ptr, const int32
   g->nnz = nnz;
   g->flags = flags;
   int *d_flag = nullptr;
-  cudaError_t e = cudaMalloc(&d_flag, sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&d_flag, sizeof(int));
   if (e != cudaSuccess) {
     graph_free(g);
-    return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
+    return cuda_fail(e, "tbfs::dev_alloc(flag)", __LINE__);
   }
   st = build_csc(g, col_ptr, row_idx, d_flag);
   if (st == TBFS_OK) st = finish_lists(g, d_flag);
-  cudaFree(d_flag);
+  tbfs::dev_free(d_flag);
   if (st == TBFS_OK) st = graph_finish(g);
   if (st != TBFS_OK) {
     graph_free(g);
@@ -272,18 +276,18 @@ static tbfs_status build_cooc(tbfs_graph *g, const int32_t *row, const int32_t *
   const cudaMemcpyKind kind = (g->flags & TBFS_GRAPH_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice
                                                                   : cudaMemcpyHostToDevice;
   int *dr = nullptr, *dc = nullptr;
-  cudaError_t e = cudaMalloc(&dr, (nnz ? nnz : 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&dc, (nnz ? nnz : 1) * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&dr, (nnz ? nnz : 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&dc, (nnz ? nnz : 1) * sizeof(int));
   if (e == cudaSuccess && nnz) e = cudaMemcpy(dr, row, nnz * sizeof(int), kind);
   if (e == cudaSuccess && nnz) e = cudaMemcpy(dc, col, nnz * sizeof(int), kind);
   if (e == cudaSuccess) e = cudaMemset(d_flag, 0, sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&g->cp, (n + 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&g->ic, (nnz ? nnz : 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&g->cp, (n + 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&g->ic, (nnz ? nnz : 1) * sizeof(int));
   /* in-lists: key = column (target), value = row (source) */
   if (e == cudaSuccess)
     e = tbfs::counting_sort_lists(dc, dr, g->nnz, g->n, g->cp, g->ic, d_flag, 0);
-  cudaFree(dr);
-  cudaFree(dc);
+  tbfs::dev_free(dr);
+  tbfs::dev_free(dc);
   if (e != cudaSuccess) return cuda_fail(e, "COOC ingest", __LINE__);
   int flag = 0;
   tbfs_status st = read_flag(d_flag, 0, &flag);
@@ -307,13 +311,13 @@ extern "C" tbfs_status tbfs_graph_create_cooc(const int32_t *row, const int32_t 
   g->nnz = nnz;
   g->flags = flags;
   int *d_flag = nullptr;
-  cudaError_t e = cudaMalloc(&d_flag, sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&d_flag, sizeof(int));
   if (e != cudaSuccess) {
     graph_free(g);
-    return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
+    return cuda_fail(e, "tbfs::dev_alloc(flag)", __LINE__);
   }
   st = build_cooc(g, row, col, d_flag);
-  cudaFree(d_flag);
+  tbfs::dev_free(d_flag);
   if (st == TBFS_OK) st = graph_finish(g);
   if (st != TBFS_OK) {
     graph_free(g);
@@ -358,14 +362,14 @@ static tbfs_status graph_from_device_edges(const int *d_src, const int *d_dst, i
   }
   g->nnz = nnz;
   int *d_flag = nullptr;
-  e = cudaMalloc(&d_flag, sizeof(int));
+  e = tbfs::dev_alloc(&d_flag, sizeof(int));
   if (e != cudaSuccess) {
     graph_free(g);
-    return cuda_fail(e, "cudaMalloc(flag)", __LINE__);
+    return cuda_fail(e, "tbfs::dev_alloc(flag)", __LINE__);
   }
   cudaMemset(d_flag, 0, sizeof(int));
   tbfs_status st = finish_lists(g, d_flag);
-  cudaFree(d_flag);
+  tbfs::dev_free(d_flag);
   if (st == TBFS_OK) st = graph_finish(g);
   if (st != TBFS_OK) {
     graph_free(g);
@@ -392,13 +396,13 @@ extern "C" tbfs_status tbfs_graph_create_edges(const int32_t *src, const int32_t
     return graph_from_device_edges(src, dst, n, m, build_flags, graph_flags, out);
   int *ds = nullptr, *dd = nullptr;
   const size_t bytes = (size_t)(m > 0 ? m : 1) * sizeof(int);
-  cudaError_t e = cudaMalloc(&ds, bytes);
-  if (e == cudaSuccess) e = cudaMalloc(&dd, bytes);
+  cudaError_t e = tbfs::dev_alloc(&ds, bytes);
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&dd, bytes);
   if (e == cudaSuccess && m > 0) e = cudaMemcpy(ds, src, (size_t)m * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && m > 0) e = cudaMemcpy(dd, dst, (size_t)m * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) st = graph_from_device_edges(ds, dd, n, m, build_flags, graph_flags, out);
-  cudaFree(ds);
-  cudaFree(dd);
+  tbfs::dev_free(ds);
+  tbfs::dev_free(dd);
   if (e != cudaSuccess) return cuda_fail(e, "edge list upload", __LINE__);
   return st;
 }
@@ -469,13 +473,13 @@ extern "C" tbfs_status tbfs_graph_create_mm(const char *text, int64_t bytes, int
   char *dt = nullptr;
   int *ds = nullptr, *dd = nullptr;
   const size_t eb = (size_t)(nz > 0 ? nz : 1) * sizeof(int);
-  cudaError_t e = cudaMalloc(&dt, (size_t)(len > 0 ? len : 1));
-  if (e == cudaSuccess) e = cudaMalloc(&ds, eb);
-  if (e == cudaSuccess) e = cudaMalloc(&dd, eb);
+  cudaError_t e = tbfs::dev_alloc(&dt, (size_t)(len > 0 ? len : 1));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&ds, eb);
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&dd, eb);
   if (e == cudaSuccess && len > 0) e = cudaMemcpy(dt, text + data, (size_t)len, cudaMemcpyHostToDevice);
   long long lines = 0, bad = -1;
   if (e == cudaSuccess) e = tbfs::mm_parse_device(dt, len, nz, M, N, ds, dd, &lines, &bad, 0);
-  cudaFree(dt);
+  tbfs::dev_free(dt);
   if (e == cudaSuccess) {
     if (lines < nz) {
       tbfs_set_error("Matrix Market text ends after %lld of %lld entries", lines, nz);
@@ -487,8 +491,8 @@ extern "C" tbfs_status tbfs_graph_create_mm(const char *text, int64_t bytes, int
       st = graph_from_device_edges(ds, dd, (int32_t)N, nz, build_flags, graph_flags, out);
     }
   }
-  cudaFree(ds);
-  cudaFree(dd);
+  tbfs::dev_free(ds);
+  tbfs::dev_free(dd);
   if (e != cudaSuccess) return cuda_fail(e, "Matrix Market parse on the device", __LINE__);
   return st;
 }
@@ -547,13 +551,13 @@ extern "C" tbfs_status tbfs_graph_get_cooc(const tbfs_graph *g, int32_t *row, in
   if (g->nnz == 0) return TBFS_OK;
   CUDA_TRY(cudaSetDevice(g->device));
   int *dcol = nullptr;
-  CUDA_TRY(cudaMalloc(&dcol, (size_t)g->nnz * sizeof(int)));
+  CUDA_TRY(tbfs::dev_alloc(&dcol, (size_t)g->nnz * sizeof(int)));
   cudaError_t e = tbfs::expand_columns(g->cp, g->n, dcol, 0);
   if (e == cudaSuccess)
     e = cudaMemcpy(col, dcol, (size_t)g->nnz * sizeof(int), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess)
     e = cudaMemcpy(row, g->ic, (size_t)g->nnz * sizeof(int), cudaMemcpyDeviceToHost);
-  cudaFree(dcol);
+  tbfs::dev_free(dcol);
   if (e != cudaSuccess) return cuda_fail(e, "tbfs_graph_get_cooc", __LINE__);
   return TBFS_OK;
 }
@@ -687,9 +691,9 @@ static tbfs_status stats_from(const BfsCtl &c, cudaEvent_t ev0, cudaEvent_t ev1,
 }
 
 static tbfs_status ensure_result_buffers(tbfs_graph *g, bool sigma) {
-  if (!g->S_dev) CUDA_TRY(cudaMalloc(&g->S_dev, (size_t)g->n * sizeof(int)));
+  if (!g->S_dev) CUDA_TRY(tbfs::dev_alloc(&g->S_dev, (size_t)g->n * sizeof(int)));
   if (sigma && !g->sigma_dev)
-    CUDA_TRY(cudaMalloc(&g->sigma_dev, (size_t)g->n * sizeof(unsigned long long)));
+    CUDA_TRY(tbfs::dev_alloc(&g->sigma_dev, (size_t)g->n * sizeof(unsigned long long)));
   return TBFS_OK;
 }
 
@@ -730,10 +734,10 @@ extern "C" tbfs_status tbfs_bfs(tbfs_graph *g, int32_t root, const tbfs_options 
   const bool tracing = o.level_trace != nullptr && o.level_trace_cap >= 2;
   if (tracing) {
     if (g->trace_cap < o.level_trace_cap) {
-      cudaFree(g->trace_dev);
+      tbfs::dev_free(g->trace_dev);
       g->trace_dev = nullptr;
       g->trace_cap = 0;
-      CUDA_TRY(cudaMalloc(&g->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long)));
+      CUDA_TRY(tbfs::dev_alloc(&g->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long)));
       g->trace_cap = o.level_trace_cap;
     }
     CUDA_TRY(cudaMemsetAsync(g->trace_dev, 0, (size_t)o.level_trace_cap * 4 * sizeof(long long), s));
@@ -762,6 +766,30 @@ extern "C" tbfs_status tbfs_bfs(tbfs_graph *g, int32_t root, const tbfs_options 
   return TBFS_OK;
 }
 
+/* Per-root control blocks and events of tbfs_bfs_many, grown to k roots. */
+static tbfs_status many_reserve(tbfs_graph *g, int32_t k) {
+  if (g->many_cap >= k) return TBFS_OK;
+  tbfs::dev_free(g->many_ctl);
+  g->many_ctl = nullptr;
+  if (g->many_ctl_host) cudaFreeHost(g->many_ctl_host);
+  g->many_ctl_host = nullptr;
+  g->many_cap = 0;
+  CUDA_TRY(tbfs::dev_alloc(&g->many_ctl, (size_t)k * sizeof(BfsCtl)));
+  CUDA_TRY(cudaMallocHost(&g->many_ctl_host, (size_t)k * sizeof(BfsCtl)));
+  while (g->many_ev.size() < 2 * (size_t)k) {
+    cudaEvent_t x = nullptr;
+    CUDA_TRY(cudaEventCreate(&x));
+    g->many_ev.push_back(x);
+  }
+  while (g->many_sync.size() < 2 * (size_t)k) {
+    cudaEvent_t x = nullptr;
+    CUDA_TRY(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    g->many_sync.push_back(x);
+  }
+  g->many_cap = k;
+  return TBFS_OK;
+}
+
 extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_t k,
                                      const tbfs_options *opt, int32_t *S, int64_t *sigma,
                                      tbfs_stats *stats) {
@@ -781,20 +809,18 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
    * the copy stream while root i+1 is traversed on s */
   if (host_out) {
     if ((st = ensure_result_buffers(g, want_sigma)) != TBFS_OK) return st;
-    if (!g->S_dev2) CUDA_TRY(cudaMalloc(&g->S_dev2, (size_t)g->n * sizeof(int)));
+    if (!g->S_dev2) CUDA_TRY(tbfs::dev_alloc(&g->S_dev2, (size_t)g->n * sizeof(int)));
     if (want_sigma && !g->sigma_dev2)
-      CUDA_TRY(cudaMalloc(&g->sigma_dev2, (size_t)g->n * sizeof(unsigned long long)));
+      CUDA_TRY(tbfs::dev_alloc(&g->sigma_dev2, (size_t)g->n * sizeof(unsigned long long)));
     if (!g->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
   }
-  std::vector<cudaEvent_t> ev(2 * (size_t)k, nullptr);
-  std::vector<cudaEvent_t> ready((size_t)k, nullptr), copied((size_t)k, nullptr);
-  BfsCtl *ctl_h = nullptr;
-  cudaError_t e = cudaMallocHost(&ctl_h, (size_t)k * sizeof(BfsCtl));
-  for (size_t i = 0; e == cudaSuccess && i < ev.size(); ++i) e = cudaEventCreate(&ev[i]);
-  for (int32_t i = 0; host_out && e == cudaSuccess && i < k; ++i) {
-    e = cudaEventCreateWithFlags(&ready[(size_t)i], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied[(size_t)i], cudaEventDisableTiming);
-  }
+  if ((st = many_reserve(g, k)) != TBFS_OK) return st;
+  cudaEvent_t *ev = g->many_ev.data();
+  cudaEvent_t *ready = g->many_sync.data(), *copied = ready + k;
+  BfsCtl *ctl_h = g->many_ctl_host;
+  /* the k launches need no stream operation between them but their events:
+   * every root has its own control block, all cleared here */
+  cudaError_t e = cudaMemsetAsync(g->many_ctl, 0, (size_t)k * sizeof(BfsCtl), s);
   const size_t n = (size_t)g->n;
   for (int32_t i = 0; e == cudaSuccess && st == TBFS_OK && i < k; ++i) {
     int *S_dst;
@@ -803,26 +829,31 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
       S_dst = (i & 1) ? g->S_dev2 : g->S_dev;
       sig_dst = (i & 1) ? g->sigma_dev2 : g->sigma_dev;
       /* the buffer's previous results must be on their way home first */
-      if (i >= 2) e = cudaStreamWaitEvent(s, copied[(size_t)i - 2], 0);
+      if (i >= 2) e = cudaStreamWaitEvent(s, copied[i - 2], 0);
       if (e != cudaSuccess) break;
     } else {
       S_dst = S + i * n;
       sig_dst = reinterpret_cast<unsigned long long *>(sigma) + (want_sigma ? i * n : 0);
     }
-    const BfsParams p = make_params(g, roots[i], o, S_dst, sig_dst);
-    st = enqueue_bfs(g, p, s, ev[2 * i], ev[2 * i + 1], ctl_h + i);
-    if (st == TBFS_OK && host_out) {
-      e = cudaEventRecord(ready[(size_t)i], s);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(g->copy_stream, ready[(size_t)i], 0);
+    BfsParams p = make_params(g, roots[i], o, S_dst, sig_dst);
+    p.ctl = g->many_ctl + i;
+    e = cudaEventRecord(ev[2 * i], s);
+    if (e == cudaSuccess) e = tbfs::bfs_launch(p, g->geom, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2 * i + 1], s);
+    if (e == cudaSuccess && host_out) {
+      e = cudaEventRecord(ready[i], s);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(g->copy_stream, ready[i], 0);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(S + i * n, S_dst, n * sizeof(int), cudaMemcpyDeviceToHost,
                             g->copy_stream);
       if (e == cudaSuccess && want_sigma)
         e = cudaMemcpyAsync(sigma + i * n, sig_dst, n * sizeof(int64_t), cudaMemcpyDeviceToHost,
                             g->copy_stream);
-      if (e == cudaSuccess) e = cudaEventRecord(copied[(size_t)i], g->copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(copied[i], g->copy_stream);
     }
   }
+  if (e == cudaSuccess && st == TBFS_OK)
+    e = cudaMemcpyAsync(ctl_h, g->many_ctl, (size_t)k * sizeof(BfsCtl), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && st == TBFS_OK) e = cudaStreamSynchronize(s);
   if (e == cudaSuccess && st == TBFS_OK && host_out) e = cudaStreamSynchronize(g->copy_stream);
   for (int32_t i = 0; e == cudaSuccess && st == TBFS_OK && i < k; ++i) {
@@ -832,14 +863,8 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
     g->last = tmp;
     g->depth_hint = tmp.levels;
   }
+  if (e != cudaSuccess) cudaStreamSynchronize(s); /* nothing of this call left running */
   if (host_out && g->copy_stream) cudaStreamSynchronize(g->copy_stream); /* also on error paths */
-  for (auto x : ev)
-    if (x) cudaEventDestroy(x);
-  for (auto x : ready)
-    if (x) cudaEventDestroy(x);
-  for (auto x : copied)
-    if (x) cudaEventDestroy(x);
-  if (ctl_h) cudaFreeHost(ctl_h);
   g->pending = false;
   if (e != cudaSuccess) return cuda_fail(e, "tbfs_bfs_many", __LINE__);
   return st;

@@ -54,12 +54,12 @@ namespace {
 constexpr size_t kStatBytes = (size_t)kBatchMaxRoots * (2 * sizeof(unsigned long long) + sizeof(int));
 
 void free_rows(BatchWS *w) {
-  cudaFree(w->seen);
-  cudaFree(w->F);
-  cudaFree(w->S_int);
-  cudaFree(w->sig_int);
-  cudaFree(w->hubs);
-  cudaFree(w->hub_seg);
+  tbfs::dev_free(w->seen);
+  tbfs::dev_free(w->F);
+  tbfs::dev_free(w->S_int);
+  tbfs::dev_free(w->sig_int);
+  tbfs::dev_free(w->hubs);
+  tbfs::dev_free(w->hub_seg);
   w->seen = w->F = nullptr;
   w->S_int = nullptr;
   w->sig_int = nullptr;
@@ -81,17 +81,17 @@ tbfs_status ensure_ws(tbfs_graph *g, int W, bool sigma, cudaStream_t s) {
   const size_t n = (size_t)g->n;
   if (!w->ctl) {
     w->n = g->n;
-    TRY(cudaMalloc(&w->touched, ((n + 31) / 32) * sizeof(unsigned)), "alloc");
-    TRY(cudaMalloc(&w->seg_arrive, n * sizeof(unsigned)), "alloc");
-    TRY(cudaMalloc(&w->q, 3 * n * sizeof(int)), "alloc");
-    TRY(cudaMalloc(&w->e, 3 * n * sizeof(unsigned)), "alloc");
-    TRY(cudaMalloc(&w->hq, 3 * n * sizeof(int)), "alloc");
-    TRY(cudaMalloc(&w->he, 3 * n * sizeof(unsigned)), "alloc");
-    TRY(cudaMalloc(&w->roots_dev, kBatchMaxRoots * sizeof(int)), "alloc");
+    TRY(tbfs::dev_alloc(&w->touched, ((n + 31) / 32) * sizeof(unsigned)), "alloc");
+    TRY(tbfs::dev_alloc(&w->seg_arrive, n * sizeof(unsigned)), "alloc");
+    TRY(tbfs::dev_alloc(&w->q, 3 * n * sizeof(int)), "alloc");
+    TRY(tbfs::dev_alloc(&w->e, 3 * n * sizeof(unsigned)), "alloc");
+    TRY(tbfs::dev_alloc(&w->hq, 3 * n * sizeof(int)), "alloc");
+    TRY(tbfs::dev_alloc(&w->he, 3 * n * sizeof(unsigned)), "alloc");
+    TRY(tbfs::dev_alloc(&w->roots_dev, kBatchMaxRoots * sizeof(int)), "alloc");
     TRY(cudaMallocHost(&w->roots_host, kBatchMaxRoots * sizeof(int)), "alloc");
-    TRY(cudaMalloc(&w->rst, kStatBytes), "alloc");
+    TRY(tbfs::dev_alloc(&w->rst, kStatBytes), "alloc");
     TRY(cudaMallocHost(&w->rst_host, kStatBytes), "alloc");
-    TRY(cudaMalloc(&w->ctl, sizeof(BatchCtl)), "alloc");
+    TRY(tbfs::dev_alloc(&w->ctl, sizeof(BatchCtl)), "alloc");
     TRY(cudaMallocHost(&w->ctl_host, sizeof(BatchCtl)), "alloc");
     TRY(cudaEventCreate(&w->ev0), "event");
     TRY(cudaEventCreate(&w->ev1), "event");
@@ -100,10 +100,10 @@ tbfs_status ensure_ws(tbfs_graph *g, int W, bool sigma, cudaStream_t s) {
     const bool keep_sigma = sigma || (w->sigma && w->W == W);
     free_rows(w);
     const size_t rs = 32 * (size_t)W;
-    TRY(cudaMalloc(&w->seen, n * W * sizeof(unsigned)), "alloc rows");
-    TRY(cudaMalloc(&w->F, 3 * n * W * sizeof(unsigned)), "alloc rows");
-    TRY(cudaMalloc(&w->S_int, n * rs * sizeof(int)), "alloc depth rows");
-    if (keep_sigma) TRY(cudaMalloc(&w->sig_int, n * rs * sizeof(unsigned long long)), "alloc count rows");
+    TRY(tbfs::dev_alloc(&w->seen, n * W * sizeof(unsigned)), "alloc rows");
+    TRY(tbfs::dev_alloc(&w->F, 3 * n * W * sizeof(unsigned)), "alloc rows");
+    TRY(tbfs::dev_alloc(&w->S_int, n * rs * sizeof(int)), "alloc depth rows");
+    if (keep_sigma) TRY(tbfs::dev_alloc(&w->sig_int, n * rs * sizeof(unsigned long long)), "alloc count rows");
 #ifndef TBFS_BATCH_SEG
 #define TBFS_BATCH_SEG 128
 #endif
@@ -118,14 +118,14 @@ tbfs_status ensure_ws(tbfs_graph *g, int W, bool sigma, cudaStream_t s) {
 
 tbfs_status ensure_stage(BatchWS *w, size_t entries, bool sigma) {
   if (w->stage_entries >= entries && (!sigma || w->stage_sigma)) return TBFS_OK;
-  cudaFree(w->S_stage);
-  cudaFree(w->sig_stage);
+  tbfs::dev_free(w->S_stage);
+  tbfs::dev_free(w->sig_stage);
   w->S_stage = nullptr;
   w->sig_stage = nullptr;
   w->stage_entries = 0;
   w->stage_sigma = false;
-  TRY(cudaMalloc(&w->S_stage, entries * sizeof(int)), "alloc staging");
-  if (sigma) TRY(cudaMalloc(&w->sig_stage, entries * sizeof(unsigned long long)), "alloc staging");
+  TRY(tbfs::dev_alloc(&w->S_stage, entries * sizeof(int)), "alloc staging");
+  if (sigma) TRY(tbfs::dev_alloc(&w->sig_stage, entries * sizeof(unsigned long long)), "alloc staging");
   w->stage_entries = entries;
   w->stage_sigma = sigma;
   return TBFS_OK;
@@ -138,18 +138,18 @@ int width_for(int k) { return k <= 32 ? 1 : k <= 64 ? 2 : k <= 128 ? 4 : 8; }
 void batch_ws_free(BatchWS *w) {
   if (!w) return;
   free_rows(w);
-  cudaFree(w->touched);
-  cudaFree(w->seg_arrive);
-  cudaFree(w->q);
-  cudaFree(w->e);
-  cudaFree(w->hq);
-  cudaFree(w->he);
-  cudaFree(w->roots_dev);
-  cudaFree(w->rst);
-  cudaFree(w->ctl);
-  cudaFree(w->S_stage);
-  cudaFree(w->sig_stage);
-  cudaFree(w->trace_dev);
+  tbfs::dev_free(w->touched);
+  tbfs::dev_free(w->seg_arrive);
+  tbfs::dev_free(w->q);
+  tbfs::dev_free(w->e);
+  tbfs::dev_free(w->hq);
+  tbfs::dev_free(w->he);
+  tbfs::dev_free(w->roots_dev);
+  tbfs::dev_free(w->rst);
+  tbfs::dev_free(w->ctl);
+  tbfs::dev_free(w->S_stage);
+  tbfs::dev_free(w->sig_stage);
+  tbfs::dev_free(w->trace_dev);
   if (w->roots_host) cudaFreeHost(w->roots_host);
   if (w->rst_host) cudaFreeHost(w->rst_host);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -252,10 +252,10 @@ extern "C" tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32
     const bool tracing = r0 == 0 && o.level_trace != nullptr && o.level_trace_cap >= 2;
     if (tracing) {
       if (w->trace_cap < o.level_trace_cap) {
-        cudaFree(w->trace_dev);
+        tbfs::dev_free(w->trace_dev);
         w->trace_dev = nullptr;
         w->trace_cap = 0;
-        TRY(cudaMalloc(&w->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long)), "alloc trace");
+        TRY(tbfs::dev_alloc(&w->trace_dev, (size_t)o.level_trace_cap * 4 * sizeof(long long)), "alloc trace");
         w->trace_cap = o.level_trace_cap;
       }
       TRY(cudaMemsetAsync(w->trace_dev, 0, (size_t)o.level_trace_cap * 4 * sizeof(long long), s),

@@ -1190,7 +1190,7 @@ cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_
   *nhub = 0;
   *hub_segs = 0;
   int *pos = nullptr;
-  cudaError_t e = cudaMalloc(&pos, ((size_t)n + 1) * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&pos, ((size_t)n + 1) * sizeof(int));
   if (e != cudaSuccess) return e;
   const unsigned blocks = (unsigned)(((long long)n + 1 + 255) / 256);
   hub_flag_kernel<<<blocks, 256, 0, s>>>(cp, n, seg_len, pos);
@@ -1198,8 +1198,8 @@ cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_
   int cnt = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&cnt, pos + n, sizeof(int), cudaMemcpyDeviceToHost);
   int *h = nullptr, *ns = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc(&h, ((size_t)cnt + 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&ns, ((size_t)cnt + 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&h, ((size_t)cnt + 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&ns, ((size_t)cnt + 1) * sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(ns, 0, ((size_t)cnt + 1) * sizeof(int), s);
   if (e == cudaSuccess && cnt > 0) {
     hub_fill_kernel<<<(unsigned)(((long long)n + 255) / 256), 256, 0, s>>>(cp, n, seg_len, pos, h,
@@ -1209,10 +1209,10 @@ cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_
   if (e == cudaSuccess) e = exclusive_scan(ns, (long long)cnt + 1, ns, s);
   int tot = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&tot, ns + cnt, sizeof(int), cudaMemcpyDeviceToHost);
-  cudaFree(pos);
+  tbfs::dev_free(pos);
   if (e != cudaSuccess) {
-    cudaFree(h);
-    cudaFree(ns);
+    tbfs::dev_free(h);
+    tbfs::dev_free(ns);
     return e;
   }
   *hubs = h;

@@ -431,16 +431,16 @@ struct Scratch {
   SweepCtl *ctl = nullptr;
   tbfs::BfsCtl *fctl_host = nullptr;
   ~Scratch() {
-    cudaFree(ints);
-    cudaFree(sigs);
-    cudaFree(dbls);
-    cudaFree(fill);
-    cudaFree(partial);
-    cudaFree(dl);
-    cudaFree(bc);
-    cudaFree(out);
-    cudaFree(rs);
-    cudaFree(ctl);
+    tbfs::dev_free(ints);
+    tbfs::dev_free(sigs);
+    tbfs::dev_free(dbls);
+    tbfs::dev_free(fill);
+    tbfs::dev_free(partial);
+    tbfs::dev_free(dl);
+    tbfs::dev_free(bc);
+    tbfs::dev_free(out);
+    tbfs::dev_free(rs);
+    tbfs::dev_free(ctl);
     if (fctl_host) cudaFreeHost(fctl_host);
   }
 };
@@ -475,9 +475,9 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
   const size_t nI = n + 2; /* every int array of a slot: n + 2 entries */
   const size_t ints_per_slot = 8 * nI + seg_cap;
   const size_t dbls_per_slot = n + seg_cap;
-  BTRY(cudaMalloc(&w.ints, (size_t)K * ints_per_slot * sizeof(int)), "alloc");
-  BTRY(cudaMalloc(&w.sigs, (size_t)K * n * sizeof(unsigned long long)), "alloc");
-  BTRY(cudaMalloc(&w.dbls, (size_t)K * dbls_per_slot * sizeof(double)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.ints, (size_t)K * ints_per_slot * sizeof(int)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.sigs, (size_t)K * n * sizeof(unsigned long long)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.dbls, (size_t)K * dbls_per_slot * sizeof(double)), "alloc");
   for (int j = 0; j < K; ++j) {
     Slot &x = w.slots[(size_t)j];
     int *b = w.ints + (size_t)j * ints_per_slot;
@@ -494,13 +494,13 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
     x.q = w.dbls + (size_t)j * dbls_per_slot;
     x.part = x.q + n;
   }
-  BTRY(cudaMalloc(&w.fill, (n + 1) * sizeof(int)), "alloc");
-  BTRY(cudaMalloc(&w.partial, (size_t)tbfs::scan_partials((long long)n + 2) * sizeof(int)),
+  BTRY(tbfs::dev_alloc(&w.fill, (n + 1) * sizeof(int)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.partial, (size_t)tbfs::scan_partials((long long)n + 2) * sizeof(int)),
        "alloc");
-  BTRY(cudaMalloc(&w.dl, (size_t)K * n * sizeof(double)), "alloc");
-  BTRY(cudaMalloc(&w.bc, n * sizeof(double)), "alloc");
-  BTRY(cudaMalloc(&w.rs, (size_t)K * sizeof(RootSweep)), "alloc");
-  BTRY(cudaMalloc(&w.ctl, sizeof(SweepCtl)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.dl, (size_t)K * n * sizeof(double)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.bc, n * sizeof(double)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.rs, (size_t)K * sizeof(RootSweep)), "alloc");
+  BTRY(tbfs::dev_alloc(&w.ctl, sizeof(SweepCtl)), "alloc");
   BTRY(cudaMallocHost(&w.fctl_host, sizeof(tbfs::BfsCtl)), "alloc");
   BTRY(cudaMemsetAsync(w.bc, 0, n * sizeof(double), s), "clear");
   /* grid of the sweep: all SMs, as occupancy allows (cooperative) */
@@ -617,7 +617,7 @@ extern "C" tbfs_status tbfs_brandes(tbfs_graph *g, const int32_t *roots, int32_t
   /* results in the caller's numbering */
   double *dst = bc;
   if (!o.outputs_on_device) {
-    BTRY(cudaMalloc(&w.out, n * sizeof(double)), "alloc");
+    BTRY(tbfs::dev_alloc(&w.out, n * sizeof(double)), "alloc");
     dst = w.out;
   }
   tbfs::gather_double_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w.bc, g->inv, g->n, dst);

@@ -248,11 +248,11 @@ cudaError_t exclusive_scan(const int *in, long long len, int *out, cudaStream_t 
   const long long tiles = scan_partials(len);
   if (tiles == 0) return cudaSuccess;
   int *partial = nullptr;
-  cudaError_t e = cudaMalloc(&partial, (size_t)tiles * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&partial, (size_t)tiles * sizeof(int));
   if (e != cudaSuccess) return e;
   e = exclusive_scan_ws(in, len, out, partial, s);
   cudaError_t e2 = cudaStreamSynchronize(s);
-  cudaFree(partial);
+  tbfs::dev_free(partial);
   return e != cudaSuccess ? e : e2;
 }
 
@@ -274,7 +274,7 @@ cudaError_t stable_sort_pairs(unsigned *keys, unsigned *vals, long long len, int
   const long long tiles = (len + kRadixTile - 1) / kRadixTile;
   if (tiles * 256 > INT32_MAX) return cudaErrorInvalidValue;
   int *hist = nullptr;
-  cudaError_t e = cudaMalloc(&hist, (size_t)tiles * 256 * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&hist, (size_t)tiles * 256 * sizeof(int));
   if (e != cudaSuccess) return e;
   unsigned *ka = keys, *va = vals, *kb = ktmp, *vb = vtmp;
   for (int shift = 0; shift < bits && e == cudaSuccess; shift += 8) {
@@ -297,7 +297,7 @@ cudaError_t stable_sort_pairs(unsigned *keys, unsigned *vals, long long len, int
       e = cudaMemcpyAsync(vals, va, (size_t)len * sizeof(unsigned), cudaMemcpyDeviceToDevice, s);
   }
   cudaError_t e2 = cudaStreamSynchronize(s);
-  cudaFree(hist);
+  tbfs::dev_free(hist);
   return e != cudaSuccess ? e : e2;
 }
 
@@ -316,7 +316,7 @@ cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
   /* stable: sort copies of the pairs by key, the values are the lists */
   const size_t m = (size_t)(nnz > 0 ? nnz : 1);
   unsigned *buf = nullptr;
-  if ((e = cudaMalloc(&buf, 4 * m * sizeof(unsigned))) != cudaSuccess) return e;
+  if ((e = tbfs::dev_alloc(&buf, 4 * m * sizeof(unsigned))) != cudaSuccess) return e;
   unsigned *k = buf, *v = buf + m, *kt = buf + 2 * m, *vt = buf + 3 * m;
   e = cudaMemcpyAsync(k, keys, (size_t)nnz * sizeof(int), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess)
@@ -330,7 +330,7 @@ cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
     e = cudaGetLastError();
   }
   cudaError_t e2 = cudaStreamSynchronize(s);
-  cudaFree(buf);
+  tbfs::dev_free(buf);
   return e != cudaSuccess ? e : e2;
 }
 
@@ -462,7 +462,7 @@ cudaError_t degree_group_relabel(const int *cp, const int *ic, int n, long long 
   const float inv_mean2 = nnz > 0 ? (float)((double)n / (2.0 * (double)nnz)) : 0.0f;
   int *counts = nullptr;
   const size_t nslots = (size_t)kGroups * nblocks;
-  cudaError_t e = cudaMalloc(&counts, (nslots + 1) * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&counts, (nslots + 1) * sizeof(int));
   if (e != cudaSuccess) return e;
   group_count_kernel<<<nblocks, 32, 0, s>>>(cp, n, inv_mean2, counts);
   e = cudaGetLastError();
@@ -482,7 +482,7 @@ cudaError_t degree_group_relabel(const int *cp, const int *ic, int n, long long 
       if (e == cudaSuccess) e = cudaMemsetAsync(cp2 + n, 0, sizeof(int), s);
       if (e == cudaSuccess) e = exclusive_scan(cp2, (long long)n + 1, cp2, s);
       int *longs = nullptr; /* long lists' new ids, their count after them */
-      if (e == cudaSuccess) e = cudaMalloc(&longs, ((size_t)n + 1) * sizeof(int));
+      if (e == cudaSuccess) e = tbfs::dev_alloc(&longs, ((size_t)n + 1) * sizeof(int));
       if (e == cudaSuccess) e = cudaMemsetAsync(longs + n, 0, sizeof(int), s);
       if (e == cudaSuccess) {
         permuted_short_lists_kernel<<<grid_for(n), kThreads, 0, s>>>(cp, ic, perm, inv, cp2, n,
@@ -492,11 +492,11 @@ cudaError_t degree_group_relabel(const int *cp, const int *ic, int n, long long 
         e = cudaGetLastError();
       }
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      cudaFree(longs);
+      tbfs::dev_free(longs);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     }
   }
-  cudaFree(counts);
+  tbfs::dev_free(counts);
   return e;
 }
 

@@ -231,10 +231,10 @@ cudaError_t csc_from_edges_device(const int *src, const int *dst, long long m, i
   const size_t L = (size_t)(len > 0 ? len : 1);
   unsigned *buf = nullptr;
   int *cnt = nullptr, *keep = nullptr, *dflag = nullptr, *cp = nullptr, *ic = nullptr;
-  cudaError_t e = cudaMalloc(&buf, 4 * L * sizeof(unsigned));
-  if (e == cudaSuccess) e = cudaMalloc(&keep, (L + 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&dflag, sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&cp, ((size_t)n + 1) * sizeof(int));
+  cudaError_t e = tbfs::dev_alloc(&buf, 4 * L * sizeof(unsigned));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&keep, (L + 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&dflag, sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&cp, ((size_t)n + 1) * sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(dflag, 0, sizeof(int), s);
   unsigned *key = buf, *val = buf + L, *kt = buf + 2 * L, *vt = buf + 3 * L;
   if (e == cudaSuccess && m > 0) {
@@ -263,18 +263,18 @@ cudaError_t csc_from_edges_device(const int *src, const int *dst, long long m, i
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(bad_out, dflag, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess) e = cudaMalloc(&ic, (size_t)(nnz > 0 ? nnz : 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&ic, (size_t)(nnz > 0 ? nnz : 1) * sizeof(int));
   if (e == cudaSuccess && len > 0) {
     compact_kernel<<<grid_for(len), kThreads, 0, s>>>(val, keep, cnt, len, ic);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(buf);
-  cudaFree(keep);
-  cudaFree(dflag);
+  tbfs::dev_free(buf);
+  tbfs::dev_free(keep);
+  tbfs::dev_free(dflag);
   if (e != cudaSuccess) {
-    cudaFree(cp);
-    cudaFree(ic);
+    tbfs::dev_free(cp);
+    tbfs::dev_free(ic);
     return e;
   }
   *cp_out = cp;
@@ -292,8 +292,8 @@ cudaError_t mm_parse_device(const char *text, long long len, long long nz, long 
   if (tiles + 1 > INT32_MAX) return cudaErrorInvalidValue;
   int *offs = nullptr;
   unsigned long long *bad = nullptr;
-  cudaError_t e = cudaMalloc(&offs, (size_t)(tiles + 1) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&bad, sizeof(unsigned long long));
+  cudaError_t e = tbfs::dev_alloc(&offs, (size_t)(tiles + 1) * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&bad, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemsetAsync(offs, 0, (size_t)(tiles + 1) * sizeof(int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0xff, sizeof(unsigned long long), s);
   if (e == cudaSuccess && tiles > 0) {
@@ -311,8 +311,8 @@ cudaError_t mm_parse_device(const char *text, long long len, long long nz, long 
     e = cudaMemcpyAsync(&lines, offs + tiles, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&b, bad, sizeof(b), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(offs);
-  cudaFree(bad);
+  tbfs::dev_free(offs);
+  tbfs::dev_free(bad);
   if (e != cudaSuccess) return e;
   *lines_out = lines;
   *bad_out = b == ~0ull ? -1 : (long long)b;

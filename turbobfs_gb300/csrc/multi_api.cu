@@ -123,16 +123,16 @@ struct tbfs_arena {
 static void arena_free(tbfs_arena *a) {
   if (!a) return;
   cudaSetDevice(a->device);
-  cudaFree(a->cp);
-  cudaFree(a->ic);
+  tbfs::dev_free(a->cp);
+  tbfs::dev_free(a->ic);
   if (!a->symmetric) {
-    cudaFree(a->rp);
-    cudaFree(a->jr);
+    tbfs::dev_free(a->rp);
+    tbfs::dev_free(a->jr);
   }
-  cudaFree(a->work);
-  cudaFree(a->inst);
-  cudaFree(a->slots);
-  cudaFree(a->ctl);
+  tbfs::dev_free(a->work);
+  tbfs::dev_free(a->inst);
+  tbfs::dev_free(a->slots);
+  tbfs::dev_free(a->ctl);
   if (a->inst_host) cudaFreeHost(a->inst_host);
   if (a->ctl_host) cudaFreeHost(a->ctl_host);
   if (a->ev0) cudaEventDestroy(a->ev0);
@@ -176,8 +176,8 @@ static tbfs_status arena_build(tbfs_arena *a, const int32_t *col_ptr, const int3
     }
   }
   const size_t ncp = (size_t)(a->nv + a->g);
-  MTRY(cudaMalloc(&a->cp, ncp * sizeof(int)), "arena alloc");
-  MTRY(cudaMalloc(&a->ic, std::max<size_t>((size_t)a->ne, 1) * sizeof(int)), "arena alloc");
+  MTRY(tbfs::dev_alloc(&a->cp, ncp * sizeof(int)), "arena alloc");
+  MTRY(tbfs::dev_alloc(&a->ic, std::max<size_t>((size_t)a->ne, 1) * sizeof(int)), "arena alloc");
   MTRY(cudaMemcpy(a->cp, col_ptr, ncp * sizeof(int), cudaMemcpyHostToDevice), "arena upload");
   if (a->ne)
     MTRY(cudaMemcpy(a->ic, row_idx, (size_t)a->ne * sizeof(int), cudaMemcpyHostToDevice),
@@ -186,8 +186,8 @@ static tbfs_status arena_build(tbfs_arena *a, const int32_t *col_ptr, const int3
     a->rp = a->cp;
     a->jr = a->ic;
   } else {
-    MTRY(cudaMalloc(&a->rp, ncp * sizeof(int)), "arena alloc");
-    MTRY(cudaMalloc(&a->jr, std::max<size_t>((size_t)a->ne, 1) * sizeof(int)), "arena alloc");
+    MTRY(tbfs::dev_alloc(&a->rp, ncp * sizeof(int)), "arena alloc");
+    MTRY(tbfs::dev_alloc(&a->jr, std::max<size_t>((size_t)a->ne, 1) * sizeof(int)), "arena alloc");
     MTRY(cudaMemcpy(a->rp, rp_all.data(), ncp * sizeof(int), cudaMemcpyHostToDevice),
          "arena upload");
     if (a->ne)
@@ -195,10 +195,10 @@ static tbfs_status arena_build(tbfs_arena *a, const int32_t *col_ptr, const int3
            "arena upload");
   }
   const int slots = std::min<int32_t>(a->g, tbfs::kMultiMaxSlots);
-  MTRY(cudaMalloc(&a->inst, (size_t)slots * sizeof(InstDesc)), "arena alloc");
+  MTRY(tbfs::dev_alloc(&a->inst, (size_t)slots * sizeof(InstDesc)), "arena alloc");
   MTRY(cudaMallocHost(&a->inst_host, (size_t)slots * sizeof(InstDesc)), "arena alloc");
-  MTRY(cudaMalloc(&a->slots, (size_t)slots * sizeof(int)), "arena alloc");
-  MTRY(cudaMalloc(&a->ctl, sizeof(MultiCtl)), "arena alloc");
+  MTRY(tbfs::dev_alloc(&a->slots, (size_t)slots * sizeof(int)), "arena alloc");
+  MTRY(tbfs::dev_alloc(&a->ctl, sizeof(MultiCtl)), "arena alloc");
   MTRY(cudaMallocHost(&a->ctl_host, sizeof(MultiCtl)), "arena alloc");
   MTRY(cudaEventCreate(&a->ev0), "event");
   MTRY(cudaEventCreate(&a->ev1), "event");
@@ -280,7 +280,7 @@ extern "C" tbfs_status tbfs_arena_bfs(tbfs_arena *a, const int32_t *roots, const
   const bool want_sigma = o.want_sigma != 0;
   cudaStream_t s = (cudaStream_t)o.stream;
   if (!a->work || (want_sigma && !a->work_sigma)) {
-    cudaFree(a->work);
+    tbfs::dev_free(a->work);
     a->work = nullptr;
     a->woff.assign((size_t)a->g, 0);
     size_t tot = 0;
@@ -288,7 +288,7 @@ extern "C" tbfs_status tbfs_arena_bfs(tbfs_arena *a, const int32_t *roots, const
       a->woff[(size_t)i] = tot;
       tot += inst_bytes(a->n[(size_t)i], want_sigma);
     }
-    MTRY(cudaMalloc(&a->work, tot), "arena traversal buffers");
+    MTRY(tbfs::dev_alloc(&a->work, tot), "arena traversal buffers");
     a->work_sigma = want_sigma;
   }
   const long long timeout = o.timeout_ns > 0 ? o.timeout_ns : 4000000000LL;
@@ -702,10 +702,10 @@ void server_loop(tbfs_server *sv) {
 void server_free(tbfs_server *sv) {
   if (!sv) return;
   cudaSetDevice(sv->device);
-  cudaFree(sv->mem);
-  cudaFree(sv->inst);
-  cudaFree(sv->slot_ids);
-  cudaFree(sv->ctl);
+  tbfs::dev_free(sv->mem);
+  tbfs::dev_free(sv->inst);
+  tbfs::dev_free(sv->slot_ids);
+  tbfs::dev_free(sv->ctl);
   if (sv->inst_host) cudaFreeHost(sv->inst_host);
   if (sv->slot_ids_host) cudaFreeHost(sv->slot_ids_host);
   if (sv->ctl_host) cudaFreeHost(sv->ctl_host);
@@ -717,14 +717,14 @@ void server_free(tbfs_server *sv) {
 tbfs_status server_init(tbfs_server *sv) {
   MTRY(cudaGetDevice(&sv->device), "cudaGetDevice");
   MTRY(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking), "stream");
-  MTRY(cudaMalloc(&sv->mem, sv->budget), "server memory pool");
+  MTRY(tbfs::dev_alloc(&sv->mem, sv->budget), "server memory pool");
   sv->pool.reset(sv->budget);
-  MTRY(cudaMalloc(&sv->inst, (size_t)sv->max_slots * sizeof(InstDesc)), "alloc");
+  MTRY(tbfs::dev_alloc(&sv->inst, (size_t)sv->max_slots * sizeof(InstDesc)), "alloc");
   MTRY(cudaMallocHost(&sv->inst_host, (size_t)sv->max_slots * sizeof(InstDesc)), "alloc");
   memset(sv->inst_host, 0, (size_t)sv->max_slots * sizeof(InstDesc));
-  MTRY(cudaMalloc(&sv->slot_ids, (size_t)sv->max_slots * sizeof(int)), "alloc");
+  MTRY(tbfs::dev_alloc(&sv->slot_ids, (size_t)sv->max_slots * sizeof(int)), "alloc");
   MTRY(cudaMallocHost(&sv->slot_ids_host, (size_t)sv->max_slots * sizeof(int)), "alloc");
-  MTRY(cudaMalloc(&sv->ctl, sizeof(MultiCtl)), "alloc");
+  MTRY(tbfs::dev_alloc(&sv->ctl, sizeof(MultiCtl)), "alloc");
   MTRY(cudaMallocHost(&sv->ctl_host, sizeof(MultiCtl)), "alloc");
   MTRY(tbfs::multi_geometry(sv->device, &sv->geom), "launch geometry");
   int *wh = nullptr;

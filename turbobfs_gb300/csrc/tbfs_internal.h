@@ -24,9 +24,22 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "tbfs.h"
 
 namespace tbfs {
+
+/* Device memory of the library (devmem.cu): a stream-ordered pool per GPU.
+ * dev_alloc's block is usable from every stream on return; dev_free waits
+ * for the device like cudaFree, then hands the block back to the pool. */
+cudaError_t dev_alloc(void **p, size_t bytes);
+cudaError_t dev_free(void *p);
+cudaError_t dev_trim(size_t keep);
+template <class T>
+inline cudaError_t dev_alloc(T **p, size_t bytes) {
+  return dev_alloc(reinterpret_cast<void **>(p), bytes);
+}
 
 /* Words of the hand-written grid barrier (device_common.cuh): the top-level
  * arrival counter and the generation word on their own 128-byte lines, then
@@ -303,6 +316,13 @@ struct tbfs_graph {
   cudaStream_t last_stream = nullptr;
   tbfs::LaunchGeom geom;
   tbfs::BatchWS *batch = nullptr; /* frontier-matrix workspace, on first use */
+  /* tbfs_bfs_many: one control block per root (cleared together, read back
+   * together) and two events per root, kept for the next call */
+  tbfs::BfsCtl *many_ctl = nullptr;
+  tbfs::BfsCtl *many_ctl_host = nullptr; /* pinned */
+  int many_cap = 0;
+  std::vector<cudaEvent_t> many_ev;   /* 2 per root, timing          */
+  std::vector<cudaEvent_t> many_sync; /* 2 per root, ready / copied  */
   int depth_hint = 0; /* levels of the last traversal of this graph (0: none yet) */
   bool pending = false; /* a traversal was enqueued and not yet collected */
   tbfs_stats last = {};

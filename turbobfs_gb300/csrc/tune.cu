@@ -106,7 +106,7 @@ extern "C" tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40,
   cudaError_t e = cudaSetDevice(g->device);
   unsigned long long *dh = nullptr;
   int *dm = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc(&dh, tbfs::kBuckets * sizeof(unsigned long long) + sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&dh, tbfs::kBuckets * sizeof(unsigned long long) + sizeof(int));
   if (e == cudaSuccess) {
     dm = reinterpret_cast<int *>(dh + tbfs::kBuckets);
     e = cudaMemset(dh, 0, tbfs::kBuckets * sizeof(unsigned long long) + sizeof(int));
@@ -120,7 +120,7 @@ extern "C" tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40,
   int mx = 0;
   if (e == cudaSuccess) e = cudaMemcpy(h, dh, sizeof h, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(&mx, dm, sizeof mx, cudaMemcpyDeviceToHost);
-  cudaFree(dh);
+  tbfs::dev_free(dh);
   if (e != cudaSuccess) {
     tbfs_set_error("tbfs_graph_degree_profile: %s", cudaGetErrorString(e));
     return TBFS_ERR_CUDA;
@@ -159,9 +159,9 @@ extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_
   /* time one parameter set: device time of k traversals, outputs on the device */
   int *S = nullptr;
   unsigned long long *sg = nullptr;
-  if (cudaMalloc(&S, (size_t)k * g->n * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&sg, (size_t)k * g->n * sizeof(unsigned long long)) != cudaSuccess) {
-    cudaFree(S);
+  if (tbfs::dev_alloc(&S, (size_t)k * g->n * sizeof(int)) != cudaSuccess ||
+      tbfs::dev_alloc(&sg, (size_t)k * g->n * sizeof(unsigned long long)) != cudaSuccess) {
+    tbfs::dev_free(S);
     tbfs_set_error("tbfs_autotune: out of device memory for the sample outputs");
     return TBFS_ERR_OUT_OF_MEMORY;
   }
@@ -206,8 +206,8 @@ extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_
           pr = xp;
         }
       }
-  cudaFree(S);
-  cudaFree(sg);
+  tbfs::dev_free(S);
+  tbfs::dev_free(sg);
   if (st != TBFS_OK) return st;
   opt->alpha = a;
   opt->beta = b;
