@@ -676,7 +676,7 @@ def serving_report(args):
                 lat_p.append(fin - a)
             plain_span = fin - arrivals[0]
             # server: submit at the arrival times, wait for all
-            c0 = srv.counters()
+            c0, ts0 = srv.counters(), srv.time_split()
             tickets = []
             t0 = time.perf_counter()
             for a, gi, r in zip(arrivals, qg, qr):
@@ -689,7 +689,11 @@ def serving_report(args):
                 _, lat = srv.wait(tk)
                 lat_s.append(lat)
             span = time.perf_counter() - t0
-            c1 = srv.counters()
+            c1, ts1 = srv.counters(), srv.time_split()
+            nl = max(1, c1["launches"] - c0["launches"])
+            split = {k: round(ts1[k] - ts0[k], 3) for k in ("launch_ms", "plain_ms", "deliver_ms")}
+            split["routed_queries"] = ts1["plain_runs"] - ts0["plain_runs"]
+            split["mean_slots_per_launch"] = round((ts1["slot_sum"] - ts0["slot_sum"]) / nl, 2)
             lat_s = np.array(lat_s)
             lat_p = np.array(lat_p) * 1e3
             sweep.append({
@@ -698,7 +702,8 @@ def serving_report(args):
                            "p99_ms": float(np.percentile(lat_s, 99)),
                            "gteps": edges_total / span / 1e9, "span_s": span,
                            "launches": c1["launches"] - c0["launches"],
-                           "levels": c1["levels"] - c0["levels"]},
+                           "levels": c1["levels"] - c0["levels"],
+                           "server_thread": split},
                 "plain_fifo": {"p50_ms": float(np.percentile(lat_p, 50)),
                                "p99_ms": float(np.percentile(lat_p, 99)),
                                "gteps": edges_total / plain_span / 1e9, "span_s": plain_span},

@@ -275,6 +275,14 @@ tbfs_status tbfs_server_wait(tbfs_server *s, uint64_t ticket, tbfs_stats *stats,
                              double *latency_ms);
 tbfs_status tbfs_server_counters(tbfs_server *s, int64_t *launches, int64_t *levels,
                                  int64_t *completed);
+/* Where the server's time went (host wall clock, ms, cumulative): its
+ * thread in multi-instance launches (enqueue to completion) and in routed
+ * single-source queries; its delivery thread copying finished results to
+ * the callers' arrays, which overlaps the next launches; the number of
+ * routed queries, and the sum over launches of the slots each one ran
+ * (divided by launches: mean batch width). */
+tbfs_status tbfs_server_time_split(tbfs_server *s, double *launch_ms, double *plain_ms,
+                                   double *deliver_ms, int64_t *plain_runs, int64_t *slot_sum);
 void tbfs_server_destroy(tbfs_server *s);
 
 /* One BFS that allocates nothing.  No counterpart in the reference: it is

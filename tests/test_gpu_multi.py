@@ -160,6 +160,23 @@ def test_server_tight_memory_and_threads(gpu_available, served_graphs):
             assert res.sigma is None
 
 
+def test_server_burst_waited_in_reverse(gpu_available, served_graphs):
+    """A burst larger than the memory budget, waited for newest first: the
+    delivery of finished queries frees their memory without any waiter, so
+    the queued ones are admitted and nothing deadlocks."""
+    hs, gs = served_graphs
+    qs = _queries(hs, 40, seed=3)
+    need = max(48 * h.n for h in hs)
+    with tb.Server(max_slots=4, mem_budget=2 * need) as srv:
+        tickets = [srv.submit(gs[gi], r) for gi, r in qs]
+        results = {t: srv.wait(t) for t in reversed(tickets)}
+        assert srv.counters()["completed"] == len(qs)
+    for (gi, r), t in zip(qs, tickets):
+        res, _ = results[t]
+        alone = gs[gi].bfs(r)
+        assert np.array_equal(res.S, alone.S) and np.array_equal(res.sigma, alone.sigma)
+
+
 def test_server_rejects_and_oversized(gpu_available, served_graphs):
     hs, gs = served_graphs
     with tb.Server(max_slots=2, mem_budget=256 << 10) as srv:
@@ -186,7 +203,11 @@ def test_server_routes_large_shallow_and_deep_graphs(gpu_available):
             first = srv.wait(srv.submit(gs[1], qs[1][1]))  # learns the grid's depth
             tickets = [srv.submit(gs[gi], r) for gi, r in qs]
             results = [srv.wait(t) for t in tickets]
+            split, c = srv.time_split(), srv.counters()
         assert first[0].stats["levels"] > 48
+        # the first grid query and the six scale-18 ones take the single-source route
+        assert split["plain_runs"] >= 7 and split["launch_ms"] > 0 and split["deliver_ms"] > 0
+        assert split["slot_sum"] >= c["launches"] >= 1
         for (gi, r), (res, _) in zip(qs, results):
             alone = gs[gi].bfs(r)
             assert np.array_equal(res.S, alone.S) and np.array_equal(res.sigma, alone.sigma)

@@ -114,6 +114,8 @@ _SIGNATURES = {
                                    POINTER(c_uint64)]),
     "tbfs_server_wait": (c_int, [c_void_p, c_uint64, POINTER(Stats), POINTER(c_double)]),
     "tbfs_server_counters": (c_int, [c_void_p, _P_I64, _P_I64, _P_I64]),
+    "tbfs_server_time_split": (c_int, [c_void_p, POINTER(c_double), POINTER(c_double), POINTER(c_double),
+                                        POINTER(c_int64), POINTER(c_int64)]),
     "tbfs_server_destroy": (None, [c_void_p]),
     "tbfs_bfs_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64,
                                  c_int32, c_int32, c_void_p, c_void_p, c_void_p,

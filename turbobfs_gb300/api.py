@@ -396,6 +396,15 @@ class Server:
                                          ctypes.byref(c)), "tbfs_server_counters")
         return {"launches": a.value, "levels": b.value, "completed": c.value}
 
+    def time_split(self) -> dict:
+        """Host wall time of the server thread by activity (ms, cumulative)."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        d, e = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().tbfs_server_time_split(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                           ctypes.byref(d), ctypes.byref(e)), "tbfs_server_time_split")
+        return {"launch_ms": a.value, "plain_ms": b.value, "deliver_ms": c.value,
+                "plain_runs": d.value, "slot_sum": e.value}
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
             lib().tbfs_server_destroy(self._h)

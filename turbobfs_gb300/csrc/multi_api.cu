@@ -424,6 +424,19 @@ struct Slot {
   size_t off = 0, bytes = 0;
 };
 
+/* A finished multi-instance query whose results were gathered into caller
+ * order on the server's stream (event `ready`): the delivery thread copies
+ * them to the caller's arrays and then returns the memory block. */
+struct Delivery {
+  std::shared_ptr<Request> r;
+  cudaEvent_t ready = nullptr;
+  const int *S_c = nullptr;
+  const unsigned long long *sig_c = nullptr;
+  int n = 0;
+  size_t off = 0, bytes = 0;
+  tbfs_stats stats = {};
+};
+
 }  // namespace
 
 struct tbfs_server {
@@ -452,8 +465,23 @@ struct tbfs_server {
   bool stop = false;
   tbfs_status fatal = TBFS_OK;
   std::thread worker;
+  /* result delivery, off the server thread: copies of finished queries run
+   * while the next launch does */
+  std::deque<Delivery> deliveries;
+  std::vector<cudaEvent_t> free_events;
+  std::condition_variable cv_deliver;
+  /* delivery threads (kDeliverThreads), each with its own copy stream */
+  std::vector<cudaStream_t> copy_streams;
+  std::vector<std::thread> deliverers;
+  bool deliver_stop = false;
+  bool mem_blocked = false; /* admission waits for memory that deliveries hold */
   /* counters */
   long long launches = 0, levels_run = 0, completed = 0, plain_runs = 0;
+  /* host wall time, ns: the server thread in multi-instance launches (enqueue
+   * to synchronisation) and in routed single-source queries; the delivery
+   * thread copying finished results (overlaps the launches); slot_sum = sum
+   * over launches of the slots run */
+  long long launch_ns = 0, plain_ns = 0, deliver_ns = 0, slot_sum = 0;
   double device_ms = 0.0;
 };
 
@@ -466,31 +494,96 @@ namespace {
  * many -- shares the multi-instance launches.  The depth is that of the
  * graph's last traversal (unknown before the first: then size decides). */
 constexpr int kPlainMinVertices = 1 << 17;
+/* result-delivery threads per server: four measured worse than one (400 q/s
+ * over 64 graphs: p50 559 vs 27 ms), their pageable copies holding up the
+ * server thread's launches */
+constexpr int kDeliverThreads = 1;
 constexpr int kPlainMaxLevels = 48;
 
 bool route_plain(const tbfs_graph *g) {
   return g->n >= kPlainMinVertices && (g->depth_hint == 0 || g->depth_hint <= kPlainMaxLevels);
 }
 
-/* run one routed query to completion on the server's stream */
+/* Run one routed query on the server's stream.  Its results go to a block of
+ * the server's memory and reach the caller through the delivery thread, so
+ * the next launch does not wait for the copies; without a free block the
+ * query copies straight to the caller's arrays. */
 void run_plain(tbfs_server *sv, const std::shared_ptr<Request> &r) {
   tbfs_options o = sv->opt;
   o.want_sigma = r->sigma != nullptr;
-  o.outputs_on_device = 0;
   o.stream = sv->stream;
   o.level_trace = nullptr;
   o.level_trace_cap = 0;
+  const size_t n = (size_t)r->g->n;
+  const size_t need = align256(n * 4) + (r->sigma ? align256(n * 8) : 0);
+  size_t off = 0;
+  bool staged = false;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    staged = need <= sv->budget && sv->pool.alloc(need, &off);
+  }
+  const auto t0 = std::chrono::steady_clock::now();
   tbfs_stats st = {};
-  const tbfs_status rc = tbfs_bfs(r->g, r->root, &o, r->S, r->sigma, &st);
+  tbfs_status rc;
+  Delivery dv;
+  if (staged) {
+    o.outputs_on_device = 1;
+    int *S_d = reinterpret_cast<int *>(sv->mem + off);
+    int64_t *sig_d = r->sigma ? reinterpret_cast<int64_t *>(sv->mem + off + align256(n * 4)) : nullptr;
+    rc = tbfs_bfs(r->g, r->root, &o, S_d, sig_d, &st);
+    cudaError_t e = cudaSuccess;
+    if (rc == TBFS_OK) {
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (!sv->free_events.empty()) {
+          dv.ready = sv->free_events.back();
+          sv->free_events.pop_back();
+        }
+      }
+      if (!dv.ready) e = cudaEventCreateWithFlags(&dv.ready, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(dv.ready, sv->stream);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = TBFS_ERR_CUDA;
+      }
+    }
+    if (rc == TBFS_OK) {
+      dv.r = r;
+      dv.S_c = S_d;
+      dv.sig_c = reinterpret_cast<const unsigned long long *>(sig_d);
+      dv.n = (int)n;
+      dv.off = off;
+      dv.bytes = need;
+      dv.stats = st;
+    } else {
+      cudaStreamSynchronize(sv->stream);
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->pool.release(off, need);
+      if (dv.ready) sv->free_events.push_back(dv.ready);
+    }
+  } else {
+    o.outputs_on_device = 0;
+    rc = tbfs_bfs(r->g, r->root, &o, r->S, r->sigma, &st);
+  }
   const auto now = std::chrono::steady_clock::now();
-  std::lock_guard<std::mutex> lk(sv->mu);
-  r->stats = st;
-  r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
-  r->status = rc;
-  r->done = true;
-  sv->completed++;
-  sv->plain_runs++;
-  sv->cv_done.notify_all();
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->plain_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(now - t0).count();
+    sv->plain_runs++;
+    if (staged && rc == TBFS_OK) {
+      sv->deliveries.push_back(std::move(dv));
+    } else {
+      r->stats = st;
+      r->latency_ms = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
+      r->status = rc;
+      r->done = true;
+      sv->completed++;
+    }
+  }
+  if (staged && rc == TBFS_OK)
+    sv->cv_deliver.notify_one();
+  else
+    sv->cv_done.notify_all();
 }
 
 /* one step of the loop: admit, advance every instance up to max_phases
@@ -500,6 +593,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
   int waiting = 0;
   {
     std::unique_lock<std::mutex> lk(sv->mu);
+    sv->mem_blocked = false;
     while (!sv->pending.empty()) {
       auto &r = sv->pending.front();
       if (route_plain(r->g)) {
@@ -526,7 +620,10 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
         sv->cv_done.notify_all();
         continue;
       }
-      if (!sv->pool.alloc(need, &off)) break; /* wait for memory to be released */
+      if (!sv->pool.alloc(need, &off)) { /* wait for memory to be released */
+        sv->mem_blocked = true;
+        break;
+      }
       Slot &sl = sv->slots[(size_t)free_slot];
       sl.busy = true;
       sl.req = r;
@@ -586,6 +683,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
   p.timeout_ns = sv->opt.timeout_ns > 0 ? sv->opt.timeout_ns : 4000000000LL;
   p.wake = waiting > 0 ? nullptr : sv->wake_dev;
   p.stop_on_done = 1;
+  const auto t_launch = std::chrono::steady_clock::now();
   MTRY(cudaMemsetAsync(sv->ctl, 0, sizeof(MultiCtl), s), "clear control block");
   MTRY(tbfs::multi_launch(p, sv->geom, s), "multi launch");
   MTRY(cudaMemcpyAsync(sv->inst_host, sv->inst, (size_t)nslots * sizeof(InstDesc),
@@ -594,50 +692,106 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
   MTRY(cudaMemcpyAsync(sv->ctl_host, sv->ctl, sizeof(MultiCtl), cudaMemcpyDeviceToHost, s),
        "read control block");
   MTRY(cudaStreamSynchronize(s), "server step");
-  sv->launches++;
-  sv->levels_run += sv->ctl_host->phases;
+  const auto t_deliver = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->launches++;
+    sv->levels_run += sv->ctl_host->phases;
+    sv->slot_sum += nslots;
+    sv->launch_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(t_deliver - t_launch).count();
+  }
   if (sv->ctl_host->status != 0) {
     tbfs_set_error("tbfs_server: grid barrier wait exceeded its budget");
     return TBFS_ERR_TIMEOUT;
   }
-  /* retire: results in the caller's numbering, into the caller's buffers */
-  std::vector<int> finished;
+  /* retire: gather each finished query into caller order on this stream and
+   * hand it to the delivery thread; its slot is free for the next launch, its
+   * memory block once the copies are done */
+  std::vector<Delivery> out;
   for (int i = 0; i < nslots; ++i) {
     Slot &sl = sv->slots[(size_t)i];
     if (!sl.busy || !sv->inst_host[i].done) continue;
     const InstDesc &D = sv->inst_host[i];
-    Request &r = *sl.req;
     /* the caller-order copy sits after the traversal buffers of the block */
     unsigned char *tail = sv->mem + sl.off + inst_bytes(D.n, D.sig != nullptr);
-    int *S_c = reinterpret_cast<int *>(tail);
-    unsigned long long *sig_c =
-        D.sig ? reinterpret_cast<unsigned long long *>(tail + align256((size_t)D.n * 4)) : nullptr;
-    MTRY(tbfs::multi_gather(D.S, D.sig, D.inv, D.n, S_c, sig_c, s), "gather");
-    MTRY(cudaMemcpyAsync(r.S, S_c, (size_t)D.n * sizeof(int), cudaMemcpyDeviceToHost, s), "copy S");
-    if (sig_c)
-      MTRY(cudaMemcpyAsync(r.sigma, sig_c, (size_t)D.n * 8, cudaMemcpyDeviceToHost, s),
-           "copy sigma");
-    finished.push_back(i);
-  }
-  if (finished.empty()) return TBFS_OK;
-  MTRY(cudaStreamSynchronize(s), "copy results");
-  const auto now = std::chrono::steady_clock::now();
-  std::lock_guard<std::mutex> lk(sv->mu);
-  for (int i : finished) {
-    Slot &sl = sv->slots[(size_t)i];
-    Request &r = *sl.req;
-    fill_stats(sv->inst_host[i], 0.0f, &r.stats);
-    r.g->depth_hint = r.stats.levels;
-    r.latency_ms = std::chrono::duration<double, std::milli>(now - r.t_submit).count();
-    r.status = TBFS_OK;
-    r.done = true;
-    sv->pool.release(sl.off, sl.bytes);
+    Delivery dv;
+    dv.S_c = reinterpret_cast<const int *>(tail);
+    dv.sig_c = D.sig ? reinterpret_cast<const unsigned long long *>(tail + align256((size_t)D.n * 4))
+                     : nullptr;
+    MTRY(tbfs::multi_gather(D.S, D.sig, D.inv, D.n, const_cast<int *>(dv.S_c),
+                            const_cast<unsigned long long *>(dv.sig_c), s),
+         "gather");
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      if (!sv->free_events.empty()) {
+        dv.ready = sv->free_events.back();
+        sv->free_events.pop_back();
+      }
+    }
+    if (!dv.ready) MTRY(cudaEventCreateWithFlags(&dv.ready, cudaEventDisableTiming), "event");
+    MTRY(cudaEventRecord(dv.ready, s), "event");
+    dv.r = sl.req;
+    dv.n = D.n;
+    dv.off = sl.off;
+    dv.bytes = sl.bytes;
+    fill_stats(D, 0.0f, &dv.stats);
+    dv.r->g->depth_hint = dv.stats.levels;
     sl.busy = false;
     sl.req.reset();
-    sv->completed++;
+    out.push_back(std::move(dv));
   }
-  sv->cv_done.notify_all();
+  if (out.empty()) return TBFS_OK;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    for (auto &dv : out) sv->deliveries.push_back(std::move(dv));
+  }
+  if (out.size() > 1)
+    sv->cv_deliver.notify_all();
+  else
+    sv->cv_deliver.notify_one();
   return TBFS_OK;
+}
+
+/* Copies finished results to the callers' arrays on the copy stream, in the
+ * order they finished, then completes the requests and frees their memory.
+ * Returns once stopped and drained. */
+void deliver_loop(tbfs_server *sv, int idx) {
+  cudaSetDevice(sv->device);
+  cudaStream_t cs = sv->copy_streams[(size_t)idx];
+  for (;;) {
+    Delivery dv;
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      sv->cv_deliver.wait(lk, [&] { return sv->deliver_stop || !sv->deliveries.empty(); });
+      if (sv->deliveries.empty()) return;
+      dv = std::move(sv->deliveries.front());
+      sv->deliveries.pop_front();
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaError_t e = cudaStreamWaitEvent(cs, dv.ready, 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dv.r->S, dv.S_c, (size_t)dv.n * sizeof(int), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess && dv.sig_c)
+      e = cudaMemcpyAsync(dv.r->sigma, dv.sig_c, (size_t)dv.n * 8, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+    if (e != cudaSuccess) cudaGetLastError();
+    const auto now = std::chrono::steady_clock::now();
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      Request &r = *dv.r;
+      r.stats = dv.stats;
+      r.latency_ms = std::chrono::duration<double, std::milli>(now - r.t_submit).count();
+      r.status = e == cudaSuccess ? TBFS_OK : TBFS_ERR_CUDA;
+      r.done = true;
+      sv->pool.release(dv.off, dv.bytes);
+      sv->free_events.push_back(dv.ready);
+      sv->completed++;
+      sv->deliver_ns += std::chrono::duration_cast<std::chrono::nanoseconds>(now - t0).count();
+      sv->mem_blocked = false;
+    }
+    sv->cv_done.notify_all();
+    sv->cv_work.notify_one();
+  }
 }
 
 void server_loop(tbfs_server *sv) {
@@ -648,7 +802,8 @@ void server_loop(tbfs_server *sv) {
       bool any_busy = false;
       for (const Slot &sl : sv->slots) any_busy |= sl.busy;
       sv->cv_work.wait(lk, [&] {
-        return sv->stop || !sv->pending.empty() || !sv->plain_q.empty() || any_busy;
+        return sv->stop || (!sv->pending.empty() && !sv->mem_blocked) || !sv->plain_q.empty() ||
+               any_busy;
       });
       if (sv->stop && sv->pending.empty() && sv->plain_q.empty() && !any_busy) return;
       if (sv->stop) {
@@ -711,12 +866,19 @@ void server_free(tbfs_server *sv) {
   if (sv->ctl_host) cudaFreeHost(sv->ctl_host);
   if (sv->wake_host) cudaFreeHost(const_cast<int *>(sv->wake_host));
   if (sv->stream) cudaStreamDestroy(sv->stream);
+  for (cudaStream_t x : sv->copy_streams) cudaStreamDestroy(x);
+  for (cudaEvent_t x : sv->free_events) cudaEventDestroy(x);
   delete sv;
 }
 
 tbfs_status server_init(tbfs_server *sv) {
   MTRY(cudaGetDevice(&sv->device), "cudaGetDevice");
   MTRY(cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking), "stream");
+  for (int i = 0; i < kDeliverThreads; ++i) {
+    cudaStream_t x = nullptr;
+    MTRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "stream");
+    sv->copy_streams.push_back(x);
+  }
   MTRY(tbfs::dev_alloc(&sv->mem, sv->budget), "server memory pool");
   sv->pool.reset(sv->budget);
   MTRY(tbfs::dev_alloc(&sv->inst, (size_t)sv->max_slots * sizeof(InstDesc)), "alloc");
@@ -763,6 +925,7 @@ extern "C" tbfs_status tbfs_server_create(int32_t max_slots, int64_t mem_budget,
     server_free(sv);
     return st;
   }
+  for (int i = 0; i < kDeliverThreads; ++i) sv->deliverers.emplace_back(deliver_loop, sv, i);
   sv->worker = std::thread(server_loop, sv);
   *out = sv;
   return TBFS_OK;
@@ -831,6 +994,19 @@ extern "C" tbfs_status tbfs_server_counters(tbfs_server *sv, int64_t *launches, 
   return TBFS_OK;
 }
 
+extern "C" tbfs_status tbfs_server_time_split(tbfs_server *sv, double *launch_ms, double *plain_ms,
+                                              double *deliver_ms, int64_t *plain_runs,
+                                              int64_t *slot_sum) {
+  if (!sv) return TBFS_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (launch_ms) *launch_ms = 1e-6 * (double)sv->launch_ns;
+  if (plain_ms) *plain_ms = 1e-6 * (double)sv->plain_ns;
+  if (deliver_ms) *deliver_ms = 1e-6 * (double)sv->deliver_ns;
+  if (plain_runs) *plain_runs = sv->plain_runs;
+  if (slot_sum) *slot_sum = sv->slot_sum;
+  return TBFS_OK;
+}
+
 extern "C" void tbfs_server_destroy(tbfs_server *sv) {
   if (!sv) return;
   {
@@ -839,5 +1015,12 @@ extern "C" void tbfs_server_destroy(tbfs_server *sv) {
   }
   sv->cv_work.notify_all();
   if (sv->worker.joinable()) sv->worker.join();
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->deliver_stop = true;
+  }
+  sv->cv_deliver.notify_all();
+  for (std::thread &t : sv->deliverers)
+    if (t.joinable()) t.join();
   server_free(sv);
 }
