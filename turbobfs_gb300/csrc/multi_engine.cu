@@ -238,11 +238,26 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
          * entries from there is searched with shuffles, edges beyond it
          * (runs of empty lists) by a binary search of their own */
         if (o0 == 0xffffffffu) o0 = dev::warp_find_owner(reinterpret_cast<const int *>(e), qn, tb);
+        /* the window's queue entries come with their prefixes; their list
+         * starts and path counts follow in one more round trip, so that an
+         * edge inside the window needs only its list entry */
         const unsigned wi = o0 + lane;
-        const unsigned ew0 = wi < qn ? __ldcg(e + wi) : 0xffffffffu;
-        const unsigned ew1 = wi + 32 < qn ? __ldcg(e + wi + 32) : 0xffffffffu;
+        const bool in0 = wi < qn, in1 = wi + 32 < qn;
+        const unsigned ew0 = in0 ? __ldcg(e + wi) : 0xffffffffu;
+        const unsigned ew1 = in1 ? __ldcg(e + wi + 32) : 0xffffffffu;
+        const int qw0 = in0 ? __ldcg(q + wi) : 0;
+        const int qw1 = in1 ? __ldcg(q + wi + 32) : 0;
         const unsigned eend = o0 + 64 < qn ? __ldcg(e + o0 + 64) : 0xffffffffu;
-        unsigned tk[kEPT], oo[kEPT], off[kEPT];
+        const int aw0 = in0 ? __ldg(rp + qw0) : 0;
+        const int aw1 = in1 ? __ldg(rp + qw1) : 0;
+        unsigned long long gw0 = 0ull, gw1 = 0ull;
+        if (sig) {
+          gw0 = in0 ? sig[qw0] : 0ull;
+          gw1 = in1 ? sig[qw1] : 0ull;
+        }
+        unsigned tk[kEPT], off[kEPT], ow[kEPT];
+        int u[kEPT], a[kEPT];
+        unsigned long long su[kEPT];
 #pragma unroll
         for (int k = 0; k < kEPT; ++k) {
           tk[k] = tb + kEPT * lane + k;
@@ -254,29 +269,47 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
             const unsigned a1 = __shfl_sync(FULL, ew1, (int)(c & 31));
             if (c < 64 && (c < 32 ? a0 : a1) <= tk[k]) j = c;
           }
-          const unsigned b0 = __shfl_sync(FULL, ew0, (int)(j & 31));
-          const unsigned b1 = __shfl_sync(FULL, ew1, (int)(j & 31));
-          const unsigned ej = j < 32 ? b0 : b1;
-          oo[k] = o0 + j;
-          off[k] = tk[k] - ej;
-          if (tk[k] < qe && tk[k] >= eend) {
-            oo[k] = lane_owner(e, qn, tk[k]);
-            off[k] = tk[k] - __ldcg(e + oo[k]);
+          const int src = (int)(j & 31);
+          const bool hi = j >= 32;
+          const unsigned b0 = __shfl_sync(FULL, ew0, src), b1 = __shfl_sync(FULL, ew1, src);
+          const int u0 = __shfl_sync(FULL, qw0, src), u1 = __shfl_sync(FULL, qw1, src);
+          const int c0 = __shfl_sync(FULL, aw0, src), c1 = __shfl_sync(FULL, aw1, src);
+          const unsigned long long g0 = __shfl_sync(FULL, gw0, src);
+          const unsigned long long g1 = __shfl_sync(FULL, gw1, src);
+          ow[k] = o0 + j;
+          off[k] = tk[k] - (hi ? b1 : b0);
+          u[k] = hi ? u1 : u0;
+          a[k] = hi ? c1 : c0;
+          su[k] = hi ? g1 : g0;
+          if (tk[k] < qe && tk[k] >= eend) { /* past the window: owner of its own */
+            const unsigned oo = lane_owner(e, qn, tk[k]);
+            ow[k] = oo;
+            off[k] = tk[k] - __ldcg(e + oo);
+            u[k] = __ldcg(q + oo);
+            a[k] = __ldg(rp + u[k]);
+            su[k] = sig ? sig[u[k]] : 0ull;
           }
         }
-        int u[kEPT], v[kEPT], sv[kEPT];
+        int v[kEPT], sv[kEPT];
         unsigned dgo[kEPT];
 #pragma unroll
-        for (int k = 0; k < kEPT; ++k) u[k] = tk[k] < qe ? __ldcg(q + oo[k]) : 0;
-#pragma unroll
-        for (int k = 0; k < kEPT; ++k)
-          v[k] = tk[k] < qe ? __ldg(jr + __ldg(rp + u[k]) + (int)off[k]) : 0;
+        for (int k = 0; k < kEPT; ++k) v[k] = tk[k] < qe ? __ldg(jr + a[k] + (int)off[k]) : 0;
 #pragma unroll
         for (int k = 0; k < kEPT; ++k) sv[k] = tk[k] < qe ? S[v[k]] : 0;
+        /* degrees of the unvisited targets, in flight with the claims */
+        int r0[kEPT], r1[kEPT];
+#pragma unroll
+        for (int k = 0; k < kEPT; ++k) {
+          r0[k] = 0;
+          r1[k] = 0;
+          if (tk[k] < qe && sv[k] == -1) {
+            r0[k] = __ldg(rp + v[k]);
+            r1[k] = __ldg(rp + v[k] + 1);
+          }
+        }
         unsigned take = 0;
 #pragma unroll
         for (int k = 0; k < kEPT; ++k) {
-          dgo[k] = 0;
           if (tk[k] < qe && sv[k] == -1) {
             sv[k] = atomicCAS(S + v[k], -1, d + 1);
             if (sv[k] == -1) {
@@ -286,13 +319,12 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
           }
         }
 #pragma unroll
-        for (int k = 0; k < kEPT; ++k)
-          if ((take >> k) & 1u) dgo[k] = (unsigned)(__ldg(rp + v[k] + 1) - __ldg(rp + v[k]));
+        for (int k = 0; k < kEPT; ++k) dgo[k] = ((take >> k) & 1u) ? (unsigned)(r1[k] - r0[k]) : 0u;
         if (sig) {
 #pragma unroll
           for (int k = 0; k < kEPT; ++k) {
             if (tk[k] < qe && sv[k] == d + 1) {
-              const unsigned long long x = sig[u[k]];
+              const unsigned long long x = su[k];
               const unsigned long long old = atomicAdd(sig + v[k], x);
               const unsigned long long s2 = old + x;
               if (s2 < old || (s2 >> 63)) ovf = true;
@@ -300,7 +332,7 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
           }
         }
         enqueue_n<kEPT>(take, v, dgo, qn_q, qn_e, ctr1);
-        o0 = __shfl_sync(FULL, oo[kEPT - 1], 31); /* owner of the round's last edge */
+        o0 = __shfl_sync(FULL, ow[kEPT - 1], 31); /* owner of the round's last edge */
       }
       if (__any_sync(FULL, ovf) && lane == 0) atomicExch(&D.ovf, 1);
       if (total <= nwarps) break;
