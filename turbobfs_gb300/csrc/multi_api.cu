@@ -470,8 +470,11 @@ struct tbfs_server {
   std::deque<Delivery> deliveries;
   std::vector<cudaEvent_t> free_events;
   std::condition_variable cv_deliver;
-  /* delivery threads (kDeliverThreads), each with its own copy stream */
+  /* delivery threads (kDeliverThreads), each with its own copy stream, two
+   * pinned staging buffers and their events */
   std::vector<cudaStream_t> copy_streams;
+  std::vector<unsigned char *> stage;   /* 2 per thread, kStageBytes each */
+  std::vector<cudaEvent_t> stage_ev;    /* 2 per thread */
   std::vector<std::thread> deliverers;
   bool deliver_stop = false;
   bool mem_blocked = false; /* admission waits for memory that deliveries hold */
@@ -494,10 +497,10 @@ namespace {
  * many -- shares the multi-instance launches.  The depth is that of the
  * graph's last traversal (unknown before the first: then size decides). */
 constexpr int kPlainMinVertices = 1 << 17;
-/* result-delivery threads per server: four measured worse than one (400 q/s
- * over 64 graphs: p50 559 vs 27 ms), their pageable copies holding up the
- * server thread's launches */
-constexpr int kDeliverThreads = 1;
+/* result-delivery threads per server, and the size of each of their two
+ * pinned staging buffers */
+constexpr int kDeliverThreads = 2;
+constexpr size_t kStageBytes = 16u << 20;
 constexpr int kPlainMaxLevels = 48;
 
 bool route_plain(const tbfs_graph *g) {
@@ -755,6 +758,33 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
 /* Copies finished results to the callers' arrays on the copy stream, in the
  * order they finished, then completes the requests and frees their memory.
  * Returns once stopped and drained. */
+/* Device -> caller's (pageable) host memory without a pageable CUDA copy:
+ * chunks go by DMA into two pinned staging buffers in turn, and each chunk is
+ * copied on by memcpy while the next one is in flight.  The CUDA driver never
+ * stages pageable memory here, so this thread's copies do not hold up the
+ * server thread's launches. */
+cudaError_t copy_to_host(tbfs_server *sv, int idx, cudaStream_t cs, void *dst, const void *src,
+                         size_t bytes) {
+  unsigned char *buf[2] = {sv->stage[2 * (size_t)idx], sv->stage[2 * (size_t)idx + 1]};
+  cudaEvent_t ev[2] = {sv->stage_ev[2 * (size_t)idx], sv->stage_ev[2 * (size_t)idx + 1]};
+  const size_t nch = (bytes + kStageBytes - 1) / kStageBytes;
+  cudaError_t e = cudaSuccess;
+  for (size_t c = 0; c <= nch && e == cudaSuccess; ++c) {
+    if (c < nch) { /* chunk c in flight into buffer c % 2 */
+      const size_t off = c * kStageBytes, len = std::min(kStageBytes, bytes - off);
+      e = cudaMemcpyAsync(buf[c & 1], static_cast<const unsigned char *>(src) + off, len,
+                          cudaMemcpyDeviceToHost, cs);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[c & 1], cs);
+    }
+    if (e == cudaSuccess && c > 0) { /* chunk c - 1 on to the caller */
+      const size_t p = c - 1, off = p * kStageBytes, len = std::min(kStageBytes, bytes - off);
+      e = cudaEventSynchronize(ev[p & 1]);
+      if (e == cudaSuccess) memcpy(static_cast<unsigned char *>(dst) + off, buf[p & 1], len);
+    }
+  }
+  return e;
+}
+
 void deliver_loop(tbfs_server *sv, int idx) {
   cudaSetDevice(sv->device);
   cudaStream_t cs = sv->copy_streams[(size_t)idx];
@@ -769,11 +799,9 @@ void deliver_loop(tbfs_server *sv, int idx) {
     }
     const auto t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamWaitEvent(cs, dv.ready, 0);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(dv.r->S, dv.S_c, (size_t)dv.n * sizeof(int), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = copy_to_host(sv, idx, cs, dv.r->S, dv.S_c, (size_t)dv.n * sizeof(int));
     if (e == cudaSuccess && dv.sig_c)
-      e = cudaMemcpyAsync(dv.r->sigma, dv.sig_c, (size_t)dv.n * 8, cudaMemcpyDeviceToHost, cs);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+      e = copy_to_host(sv, idx, cs, dv.r->sigma, dv.sig_c, (size_t)dv.n * 8);
     if (e != cudaSuccess) cudaGetLastError();
     const auto now = std::chrono::steady_clock::now();
     {
@@ -867,6 +895,10 @@ void server_free(tbfs_server *sv) {
   if (sv->wake_host) cudaFreeHost(const_cast<int *>(sv->wake_host));
   if (sv->stream) cudaStreamDestroy(sv->stream);
   for (cudaStream_t x : sv->copy_streams) cudaStreamDestroy(x);
+  for (unsigned char *b : sv->stage)
+    if (b) cudaFreeHost(b);
+  for (cudaEvent_t x : sv->stage_ev)
+    if (x) cudaEventDestroy(x);
   for (cudaEvent_t x : sv->free_events) cudaEventDestroy(x);
   delete sv;
 }
@@ -878,6 +910,14 @@ tbfs_status server_init(tbfs_server *sv) {
     cudaStream_t x = nullptr;
     MTRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking), "stream");
     sv->copy_streams.push_back(x);
+    for (int b = 0; b < 2; ++b) {
+      unsigned char *buf = nullptr;
+      MTRY(cudaMallocHost(&buf, kStageBytes), "staging buffer");
+      sv->stage.push_back(buf);
+      cudaEvent_t ev = nullptr;
+      MTRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+      sv->stage_ev.push_back(ev);
+    }
   }
   MTRY(tbfs::dev_alloc(&sv->mem, sv->budget), "server memory pool");
   sv->pool.reset(sv->budget);
