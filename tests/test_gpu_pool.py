@@ -65,3 +65,24 @@ def test_bfs_many_caches_grow_and_are_reused(gpu_available):
             assert len(stats) == k and all(st["levels"] > 0 for st in stats)
             for j, r in enumerate(roots[:k]):
                 _check(h, S[j], sg[j], r)
+
+
+def test_poisoned_batch_brandes_and_server(gpu_available, monkeypatch):
+    """Fresh blocks hold 0xA5 bytes: the frontier-matrix batch, the betweenness
+    sweep and the server still give the results of the plain path and the
+    oracle."""
+    monkeypatch.setenv("TBFS_POOL_POISON", "1")
+    h = graphs.rmat(12, 16, seed=21)
+    roots = graphs.pick_roots(h, 40, seed=21)
+    with tb.Graph.from_host_csc(h) as g:
+        S, sg, _ = g.bfs_batch(roots)
+        Sm, sgm, _ = g.bfs_many(roots)
+        assert np.array_equal(S, Sm) and np.array_equal(sg, sgm)
+        bc, _ = g.betweenness(roots[:6])
+        want, _ = oracle.brandes(h.col_ptr, h.row_idx, roots[:6])
+        assert np.array_equal(bc, want)
+        with tb.Server(max_slots=8, mem_budget=64 << 20) as srv:
+            tickets = [srv.submit(g, int(r)) for r in roots[:12]]
+            for t, j in zip(tickets, range(12)):
+                res, _ = srv.wait(t)
+                assert np.array_equal(res.S, Sm[j]) and np.array_equal(res.sigma, sgm[j])
