@@ -83,6 +83,7 @@ constexpr int kBlock = TBFS_BLOCK;
 constexpr int kWarps = kBlock / 32;
 constexpr int kWin = 128;          /* queue entries staged per warp window */
 constexpr int kEPT = TBFS_EPT;     /* most consecutive edges per lane/round */
+constexpr double kBuWordCost = 4.0; /* a bitmap word of a bottom-up level, in list entries */
 enum { DIR_TD = 0, DIR_BU = 1 };
 
 /* what an expansion does with path counts */
@@ -527,7 +528,10 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     } else if (p.mode == TBFS_MODE_BOTTOM_UP) {
       dir = DIR_BU;
     } else if (dir == DIR_TD) {
-      if ((double)qe > (double)m_u / (double)p.alpha) dir = DIR_BU;
+      /* a bottom-up level also visits every vertex's bitmap word: without
+       * that term, the tail of a deep graph (few unexplored edges left)
+       * switched to bottom-up levels three times as costly as top-down ones */
+      if ((double)qe * (double)p.alpha > (double)m_u + kBuWordCost * (double)nwords) dir = DIR_BU;
       else m_u -= qe;
     } else if (qn < prev_qn && (double)qn <= (double)p.n / (double)p.beta) {
       dir = DIR_TD;
