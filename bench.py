@@ -372,18 +372,23 @@ def run_tbfs(args, world, rank, local):
         line["e2e"] = e2e
     if cb:
         line["cpu_baseline"] = cb
-    if rank == 0 and world == 1 and not args.no_batched:
-        line["batched"] = batched_report(args)
-    if rank == 0 and world == 1 and not args.no_serving:
-        line["serving"] = serving_report(args)
-    if rank == 0 and world == 1 and not args.no_ingest:
-        line["ingest"] = ingest_report(args)
-    if rank == 0 and world == 1 and not args.no_brandes:
-        line["brandes"] = brandes_report(args)
-    if rank == 0 and world == 1 and not args.no_directed:
-        line["directed"] = directed_report(args)
-    if rank == 0 and world == 1 and not args.no_grid:
-        line["grid"] = grid_report(args)
+    # secondary reports: a failure is recorded in its own key, so that the
+    # headline line is still printed
+    reports = [("batched", batched_report, args.no_batched),
+               ("serving", serving_report, args.no_serving),
+               ("ingest", ingest_report, args.no_ingest),
+               ("brandes", brandes_report, args.no_brandes),
+               ("directed", directed_report, args.no_directed),
+               ("grid", grid_report, args.no_grid)]
+    if rank == 0 and world == 1:
+        for key, fn, skip in reports:
+            if skip:
+                continue
+            try:
+                line[key] = fn(args)
+            except Exception as exc:  # noqa: BLE001 -- reported, not swallowed
+                print(f"bench: {key} report failed: {exc!r}", file=sys.stderr, flush=True)
+                line[key] = {"error": repr(exc)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
