@@ -45,7 +45,7 @@ UNIT = "GTEPS"
 WORKLOAD = "rmat22_do_bfs_sigma_64roots"
 
 
-def parse_args():
+def parse_args(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=5)
@@ -81,7 +81,7 @@ def parse_args():
     p.add_argument("--serving-max-side", type=int, default=4096)
     p.add_argument("--serving-rates", default="100,400,1600")
     p.add_argument("--serving-queries", type=int, default=300)
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def dist_env():
