@@ -38,7 +38,7 @@ typedef enum tbfs_status {
   TBFS_ERR_TIMEOUT = 4,       /* a grid barrier wait ran past its budget    */
   TBFS_ERR_NO_DEVICE = 5,     /* no CUDA device visible                     */
   TBFS_ERR_IO = 6,            /* file could not be read / parsed            */
-  TBFS_ERR_UNSUPPORTED = 7    /* valid request this build cannot serve      */
+  TBFS_ERR_UNSUPPORTED = 7    /* valid request the library cannot serve     */
 } tbfs_status;
 
 typedef enum tbfs_mode {
@@ -310,7 +310,7 @@ tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t *d_row_idx,
 
 /* Device memory the library freed stays mapped in its pool (up to
  * TBFS_POOL_KEEP_MB, default 8192 MB, per GPU) for the next graph or
- * workspace; this hands all of it back to the driver now. */
+ * workspace; this hands all of it back to the CUDA driver now. */
 tbfs_status tbfs_release_cached_memory(void);
 
 /* Page-locked host buffers for fast host<->device copies. */

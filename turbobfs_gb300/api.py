@@ -500,5 +500,5 @@ def device_count() -> int:
 
 def release_cached_memory() -> None:
     """Hand the device memory the library's pool keeps after frees back to
-    the driver (tbfs_release_cached_memory)."""
+    the CUDA driver (tbfs_release_cached_memory)."""
     check(lib().tbfs_release_cached_memory(), "tbfs_release_cached_memory")
