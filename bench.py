@@ -248,8 +248,54 @@ def run_reference(args, world, rank):
             "config": config(h, args.roots, 1, {"sample_roots_per_step": len(sample)}),
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    try:
+        rg = reference_gpu(h, roots)
+        if rg:
+            line["reference_gpu"] = rg
+    except Exception as exc:  # noqa: BLE001 -- reported in the line
+        line["reference_gpu"] = {"error": repr(exc)}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_gpu(h, roots, k=4):
+    """The reference's own GPU kernels on this GPU (compiled unchanged for
+    sm_103a, driven by the restatement of their host loops): the
+    direction-optimizing bfs_gpu_tdbu_csc_sc kernels and the top-down
+    bfs_gpu_td_csc_sc kernels, from k of the roots; GTEPS over the sum of
+    their kernel times (the reference's own event timing of each launch).
+    None when the kernel images were not built for this machine."""
+    import oracle
+
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return None
+    except Exception:  # noqa: BLE001
+        return None
+    if not oracle.refgpu_available():
+        return None
+    deg = np.diff(h.col_ptr.astype(np.int64))
+    out = {"kernels": "TurboBFS_CSC_TDBU/bfsgputdbucsc_sc.cu and TurboBFS_CSC_TD/bfsgputdcsc_sc.cu "
+                      "(thread per column), compiled unchanged for sm_103a; the warp-per-column "
+                      "variants are not run (unsynchronised shared-memory staging)",
+           "roots": k}
+    for name, fn in (("tdbu_csc_sc", oracle.refgpu_tdbu_csc_sc),
+                     ("td_csc_sc", oracle.refgpu_td_csc_sc)):
+        fn(h.col_ptr, h.row_idx, int(roots[0]))  # warm-up (module load, first allocations)
+        ms, edges, wall = 0.0, 0, 0.0
+        for r in roots[:k]:
+            t0 = time.perf_counter()
+            res = fn(h.col_ptr, h.row_idx, int(r))
+            wall += time.perf_counter() - t0
+            S, t = res[0], res[2]
+            ms += t
+            reached = S >= 0 if name == "tdbu_csc_sc" else (S > 0) | (np.arange(h.n) == r)
+            edges += int(deg[reached].sum()) // 2
+        out[name] = {"gteps_kernels": edges / (ms * 1e-3) / 1e9, "ms_per_bfs_kernels": ms / k,
+                     "ms_per_call_wall": 1e3 * wall / k}
+    return out
 
 
 def aggregate(t_ms: float, units: float, world: int, device="cpu"):
@@ -327,6 +373,7 @@ def run_tbfs(args, world, rank, local):
         barrier()
     t_ms, units = aggregate(e0.elapsed_time(e1), args.steps * edges_per_step / 2, world, "cuda")
     value = units / (t_ms / 1e3) / 1e9
+    parity = check_results(g, roots, S_dev, sg_dev, stats, kw)
 
     # roofline of the persistent BFS kernel
     alg_bytes = []
@@ -368,6 +415,7 @@ def run_tbfs(args, world, rank, local):
         "gpu_launches": args.steps * k,
         "clocks": clk.summary(),
     }
+    line["parity"] = parity
     if e2e:
         line["e2e"] = e2e
     if cb:
@@ -389,12 +437,60 @@ def run_tbfs(args, world, rank, local):
             except Exception as exc:  # noqa: BLE001 -- reported, not swallowed
                 print(f"bench: {key} report failed: {exc!r}", file=sys.stderr, flush=True)
                 line[key] = {"error": repr(exc)}
+    line["summary"] = summary(line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     g.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def check_results(g, roots, S_dev, sg_dev, stats, params):
+    """Every timed traversal's S and sigma checked against the graph on the
+    device (tbfs_bfs_validate: level-consistent edges, a parent for every
+    reached vertex, sigma = sum of the parents' sigma), which pins both
+    vectors uniquely; runs after the timed region."""
+    bad, first = 0, None
+    for i, r in enumerate(roots):
+        v = g.validate(int(r), S_dev[i], sg_dev[i])
+        if not v["ok"] or v["visited"] != stats[i].visited or stats[i].sigma_overflow:
+            bad += 1
+            first = first if first is not None else {"root": int(r), **v}
+    out = {"roots_checked": len(roots), "mismatches": bad,
+           "checker": "tbfs_bfs_validate on the device (Graph500-style invariants, sigma = parent "
+                      "sum), on the results of the last timed step",
+           "params": params or "defaults"}
+    if first is not None:
+        out["first_failure"] = first
+    return out
+
+
+def summary(line):
+    """The headline numbers of every report in one short key, printed last."""
+    out = {"value_gteps": round(line["value"], 2), "frac": round(line["roofline"]["frac"], 4),
+           "parity_mismatches": line["parity"]["mismatches"]}
+    if "e2e" in line:
+        out["e2e_gteps"] = round(line["e2e"]["value"], 2)
+        if "dropin_pageable" in line["e2e"]:
+            out["dropin_pageable_gteps"] = round(line["e2e"]["dropin_pageable"]["value"], 2)
+    b = line.get("batched", {}).get("frontier_matrix")
+    if b:
+        out["batched_speedup_vs_plain"] = round(b["speedup_vs_plain"], 3)
+        out["batched_depths_only_speedup"] = round(b["depths_only"]["speedup_vs_plain"], 3)
+        out["batched_frac_batch_bytes"] = round(b["roofline"]["frac"], 4)
+    a = line.get("batched", {}).get("arena")
+    if a:
+        out["arena_speedup_vs_plain"] = round(a["speedup_vs_plain"], 2)
+    sv = line.get("serving", {}).get("sweep")
+    if sv:
+        out["serving_p50_p99_ms"] = {str(int(x["rate_qps"])): [round(x["server"]["p50_ms"], 2),
+                                                               round(x["server"]["p99_ms"], 2)]
+                                     for x in sv}
+    gr = line.get("grid", {}).get("auto")
+    if gr:
+        out["grid_us_per_level"] = round(gr["us_per_level"], 2)
+    return out
 
 
 def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
@@ -428,32 +524,74 @@ def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
         o.pull_ratio = o_dev.pull_ratio
         stats = (_lib.Stats * k)()
 
-        def one():
+        split = {"create_ms": 0.0, "traverse_and_copy_ms": 0.0, "destroy_ms": 0.0}
+
+        def one(acc=None):
             hdl = ctypes.c_void_p()
+            t0 = time.perf_counter()
             _lib.check(L.tbfs_graph_create_csc(ctypes.cast(p_cp, _P_I32), ctypes.cast(p_ic, _P_I32),
                                                n, nnz, _lib.GRAPH_SYMMETRIC, ctypes.byref(hdl)),
                        "tbfs_graph_create_csc")
+            t1 = time.perf_counter()
             try:
                 _lib.check(L.tbfs_bfs_many(hdl, roots_c.ctypes.data_as(_P_I32), k, ctypes.byref(o),
                                            ctypes.cast(p_S, _P_I32), ctypes.cast(p_sg, _P_I64),
                                            stats), "tbfs_bfs_many")
             finally:
+                t2 = time.perf_counter()
                 L.tbfs_graph_destroy(hdl)
+                t3 = time.perf_counter()
+            if acc is not None:
+                acc["create_ms"] += 1e3 * (t1 - t0)
+                acc["traverse_and_copy_ms"] += 1e3 * (t2 - t1)
+                acc["destroy_ms"] += 1e3 * (t3 - t2)
 
         one()  # warm
         t0 = time.perf_counter()
         for _ in range(steps):
-            one()
+            one(split)
         t = time.perf_counter() - t0
-        return {"value": world * steps * edges_per_step / 2 / t / 1e9, "unit": UNIT,
-                "h2d_bytes_per_step": 4 * (n + 1) + 4 * nnz + 4 * k,
-                "d2h_bytes_per_step": 12 * k * n,
-                "ms_per_step": 1e3 * t / steps,
-                "path": "tbfs_graph_create_csc (pinned host CSC) + tbfs_bfs_many (pinned host "
-                        "S/sigma) + tbfs_graph_destroy per step, host wall clock"}
+        dev_ms = sum(stats[i].device_ms for i in range(k))
+        split = {key: round(v / steps, 3) for key, v in split.items()}
+        split["traversals_device_ms"] = round(dev_ms, 3)
+        out = {"value": world * steps * edges_per_step / 2 / t / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": 4 * (n + 1) + 4 * nnz + 4 * k,
+               "d2h_bytes_per_step": 12 * k * n,
+               "ms_per_step": 1e3 * t / steps,
+               "split_per_step": split,
+               "path": "tbfs_graph_create_csc (pinned host CSC) + tbfs_bfs_many (pinned host "
+                       "S/sigma) + tbfs_graph_destroy per step, host wall clock"}
+        out["dropin_pageable"] = dropin_e2e(h, roots_c[:8])
+        return out
     finally:
         for b in bufs:
             L.tbfs_host_free_pinned(b)
+
+
+def dropin_e2e(h, roots):
+    """The reference's own calling pattern: one bfs_gpu_tdbu_csc_sc call per
+    root on calloc'd (pageable) host arrays (TurboBFS_CSC_TDBU/bfstdbucsc_main.c:
+    127-137,294); every call uploads the CSC, traverses, copies S and sigma back
+    and frees.  Host wall clock over the roots."""
+    import turbobfs_gb300 as tb
+
+    n, nnz = h.n, h.nnz
+    S = np.zeros(n, np.int32)
+    sg = np.zeros(n, np.int32)
+    assert tb.bfs_gpu_tdbu_csc_sc(h.row_idx, h.col_ptr, S, sg, int(roots[0]), nnz, n, 1, 1) == 0
+    edges = 0
+    deg = np.diff(h.col_ptr.astype(np.int64))
+    t0 = time.perf_counter()
+    for r in roots:
+        assert tb.bfs_gpu_tdbu_csc_sc(h.row_idx, h.col_ptr, S, sg, int(r), nnz, n, 1, 1) == 0
+    t = time.perf_counter() - t0
+    for r in roots:  # component edges of each root, outside the timed loop
+        assert tb.bfs_gpu_tdbu_csc_sc(h.row_idx, h.col_ptr, S, sg, int(r), nnz, n, 1, 1) == 0
+        edges += int(deg[S >= 0].sum()) // 2
+    return {"value": edges / t / 1e9, "unit": UNIT, "roots": len(roots),
+            "ms_per_call": 1e3 * t / len(roots),
+            "h2d_bytes_per_call": 4 * (n + 1) + 4 * nnz, "d2h_bytes_per_call": 8 * n,
+            "path": "bfs_gpu_tdbu_csc_sc with pageable numpy arrays, one call per root"}
 
 
 # ------------------------------------------------------------ batched ----

@@ -159,6 +159,32 @@ tbfs_status tbfs_graph_info(const tbfs_graph *g, int32_t *n, int64_t *nnz,
 tbfs_status tbfs_bfs(tbfs_graph *g, int32_t root, const tbfs_options *opt,
                      int32_t *S, int64_t *sigma, tbfs_stats *stats);
 
+/* Check a BFS result against the graph (a validation in the manner of the
+ * Graph500 benchmark's, run on the device).  The reference checks its GPU
+ * output by comparing it with its own sequential BFS (S_check / bfs_check,
+ * TurboBFS_CSC_TD/utils_bfs.c:93-145); S and sigma are the unique depth and
+ * path-count vectors of (g, root) exactly when no violation below is found,
+ * so this check needs no second traversal.  S (n int32, caller numbering)
+ * and sigma (n int64, may be NULL to check depths only) are device pointers
+ * when on_device, else host arrays (copied in).  Counts land in *out;
+ * TBFS_OK means the check ran, not that it passed.  Synchronous on stream
+ * (NULL = legacy default stream). */
+typedef struct tbfs_validation {
+  int64_t bad_root;       /* S[root] != 0, sigma[root] != 1, or another vertex at depth 0 */
+  int64_t bad_depth;      /* S[v] < -1                                            */
+  int64_t skips_level;    /* entries u->v with u reached and v unreached or
+                             S[v] > S[u] + 1                                      */
+  int64_t no_parent;      /* reached v != root without an in-neighbour at S[v]-1  */
+  int64_t sigma_mismatch; /* sigma[v] != sum of its parents' sigma (mod 2^64), or
+                             != 0 for an unreached v                              */
+  int64_t first_bad;      /* smallest vertex with a violation, -1 if none         */
+  int64_t visited;        /* vertices with S >= 0                                 */
+  int64_t edges;          /* in-list entries of those vertices                    */
+} tbfs_validation;
+tbfs_status tbfs_bfs_validate(tbfs_graph *g, int32_t root, const int32_t *S,
+                              const int64_t *sigma, int32_t on_device, void *stream,
+                              tbfs_validation *out);
+
 /* Statistics of the most recent traversal on g (synchronizes its stream). */
 tbfs_status tbfs_graph_last_stats(tbfs_graph *g, tbfs_stats *stats);
 
@@ -196,6 +222,41 @@ tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
  * CSC).  max_degree and mean_degree may be NULL. */
 tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40, int64_t *max_degree,
                                       double *mean_degree);
+
+/* Degree statistics of a resident graph, the numbers the reference's
+ * drivers print (TurboBFS_CSC_TD/degree.c:22-141, called from
+ * TurboBFS_CSC_TD/bfstdcsc_main.c:177-260), computed on the device.  kind:
+ *   TBFS_DEGREE_IN          in-degree (column lengths)
+ *   TBFS_DEGREE_OUT         out-degree (row counts)
+ *   TBFS_DEGREE_UNDIRECTED  degree_ug's out + in of the graph's entries: the
+ *                           column length of a TBFS_GRAPH_SYMMETRIC graph,
+ *                           in + out otherwise
+ * max_degree / argmax: degree_max (the first vertex, caller numbering, of
+ * maximum degree; -1 when every degree is 0).  mean / sd: degree_sta (sum in
+ * int64, sample standard deviation with divisor n - 1; summed in degree
+ * order, so sd agrees with the reference's vertex-order sum to rounding).
+ * dist_ac / dist_rel_ac: degree_dist_ac's accumulated log2 distribution and
+ * its percentages, bit-identical to the reference: [0] and [1] = vertices
+ * of degree 0 and 1, [b] (b >= 2) = vertices with degree in
+ * [2^(b-1), 2^b), for 2^(b-1) < max_degree only (as in degree.c, a maximum
+ * that is a power of two falls in no bucket).  dist (may be NULL) receives
+ * the per-degree counts (degree_dist) of degrees 0 .. min(dist_cap,
+ * max_degree + 1) - 1. */
+#define TBFS_DEGREE_IN 0
+#define TBFS_DEGREE_OUT 1
+#define TBFS_DEGREE_UNDIRECTED 2
+#define TBFS_DEGREE_BUCKETS 40
+typedef struct tbfs_degree_stats {
+  int64_t max_degree;
+  int64_t argmax;
+  int64_t sum;
+  double mean;
+  double sd;
+  int64_t dist_ac[TBFS_DEGREE_BUCKETS];
+  double dist_rel_ac[TBFS_DEGREE_BUCKETS];
+} tbfs_degree_stats;
+tbfs_status tbfs_graph_degree_stats(tbfs_graph *g, int32_t kind, tbfs_degree_stats *out,
+                                    int64_t *dist, int64_t dist_cap);
 
 /* Autotuner: picks alpha, beta and pull_ratio for g by timing traversals
  * from the k sample roots (device events; each parameter in turn over a
@@ -294,13 +355,17 @@ void tbfs_server_destroy(tbfs_server *s);
  * (d_out_ptr/d_out_idx; NULL for a symmetric graph), S[n] and sigma[n]
  * (sigma may be NULL for depths only).  Scratch (frontier queues, control
  * block) is a static device array inside the library sized for at most
- * TBFS_NOALLOC_MAX_VERTICES vertices (about 36 MB held on every GPU that
- * loads the library, until exit); larger n is rejected with
- * TBFS_ERR_UNSUPPORTED.  The first call on a device looks up that array's
- * device address, so make it before any stream capture.  All calls share the
- * array: calls whose GPU work overlaps race.  The input is validated on the
- * device each call; the call returns after the traversal finished on
- * `stream` (NULL = legacy default stream); stats->device_ms is left 0. */
+ * TBFS_NOALLOC_MAX_VERTICES vertices (about 36 MB held on every GPU where
+ * the library's device code is loaded, until exit); larger n is rejected
+ * with TBFS_ERR_UNSUPPORTED.  The first call on a device looks up that
+ * array's device address; since CUDA loads device code lazily, on a device
+ * where nothing else of the library ran yet it also commits the 36 MB (a
+ * warm-up call belongs before the host framework reserves device memory,
+ * and before any stream capture; without the memory the call returns
+ * TBFS_ERR_OUT_OF_MEMORY).  All calls share the array: calls whose GPU work
+ * overlaps race.  The input is validated on the device each call; the call
+ * waits for the traversal to finish on `stream` (NULL = legacy default
+ * stream) before it returns; stats->device_ms is left 0. */
 #define TBFS_NOALLOC_MAX_VERTICES (1 << 20)
 tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t *d_row_idx,
                              const int32_t *d_out_ptr, const int32_t *d_out_idx,

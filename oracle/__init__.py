@@ -52,6 +52,8 @@ def lib() -> ctypes.CDLL:
         L.oracle_seq_many.argtypes = [_P_I32, _P_I32, c_int, c_int, _P_I32, c_int, c_int,
                                       POINTER(c_double), _P_I64]
         L.oracle_seq_many.restype = c_double
+        L.oracle_degree_stats.argtypes = [_P_I32, c_int, _P_I64, _P_I64, POINTER(c_double),
+                                          POINTER(c_double), _P_I64, POINTER(c_double), c_int]
         _lib = L
     return _lib
 
@@ -166,6 +168,38 @@ def seq_many(cp, ic, roots, threads):
     return wall, secs, edges
 
 
+def degree_vectors(cp, ic, symmetric: bool):
+    """(in, out, undirected) degree vectors of a CSC graph whose column v lists
+    the sources u of edges u -> v: in = column lengths, out = row counts; the
+    undirected degree is the reference's out_degree + in_degree of the file
+    entries (TurboBFS_CSC_TD/degree.c:22-31, readMMfilef.c:56-70), which for a
+    symmetric CSC (every entry mirrored) is the column length and otherwise
+    in + out."""
+    cp = np.asarray(cp, dtype=np.int64)
+    n = cp.shape[0] - 1
+    din = np.diff(cp).astype(np.int32)
+    dout = np.bincount(np.asarray(ic, dtype=np.int64), minlength=n).astype(np.int32)
+    und = din.copy() if symmetric else (din + dout).astype(np.int32)
+    return din, dout, und
+
+
+def degree_stats(deg, cap: int = 40):
+    """Restatement of the reference's degree statistics of one degree vector:
+    {max, argmax, mean, sd, dist_ac[cap], dist_rel_ac[cap]} (tbfs_oracle.h)."""
+    deg = _i32(deg)
+    mx, ix = np.zeros(1, np.int64), np.zeros(1, np.int64)
+    mean, sd = c_double(), c_double()
+    ac = np.zeros(cap, np.int64)
+    rel = np.zeros(cap, np.float64)
+    rc = lib().oracle_degree_stats(_p(deg, _P_I32), deg.shape[0], _p(mx, _P_I64), _p(ix, _P_I64),
+                                   ctypes.byref(mean), ctypes.byref(sd), _p(ac, _P_I64),
+                                   rel.ctypes.data_as(POINTER(c_double)), cap)
+    if rc != 0:
+        raise ValueError("degree_stats: cap too small for the maximum degree")
+    return {"max": int(mx[0]), "argmax": int(ix[0]), "mean": mean.value, "sd": sd.value,
+            "dist_ac": ac, "dist_rel_ac": rel}
+
+
 # ------------------------------------------- the reference's own sources
 
 _REF_LIBS = {
@@ -174,6 +208,43 @@ _REF_LIBS = {
     "csc_tdbu": "libref_csc_tdbu.so",
     "cooc_td": "libref_cooc_td.so",
 }
+_REF_DEGREE = "libref_degree.so"
+
+
+def ref_degree_available() -> bool:
+    return (REF_DIR / _REF_DEGREE).exists()
+
+
+def ref_degree_stats(deg):
+    """The reference's own degree.c (compiled unchanged into oracle/_ref) run
+    as its driver runs it (TurboBFS_CSC_TD/bfstdcsc_main.c:177-195):
+    degree_max, degree_sta, degree_dist, degree_dist_rel, degree_dist_ac.
+    Returns the restatement's layout: dist_ac[b] = degreeDistAc[0 / 1 /
+    2^(b-1)].  Needs max >= 2 (the reference indexes degreeDistAc[1] of a
+    maxDegree-long array)."""
+    deg = _i32(deg)
+    n = deg.shape[0]
+    if "degree" not in _ref:
+        _ref["degree"] = ctypes.CDLL(str(REF_DIR / _REF_DEGREE), mode=os.RTLD_LOCAL)
+    L = _ref["degree"]
+    mx, ix = c_int(0), c_int(-1)
+    L.degree_max(_p(deg, _P_I32), ctypes.byref(mx), ctypes.byref(ix), n)
+    mean, sd = c_double(), c_double()
+    L.degree_sta(_p(deg, _P_I32), ctypes.byref(mean), ctypes.byref(sd), n)
+    m = mx.value
+    if m < 2:
+        raise ValueError("ref_degree_stats needs a maximum degree of at least 2")
+    dist = np.zeros(m + 1, np.int32)
+    rel = np.zeros(m + 1, np.float64)
+    ac = np.zeros(m, np.int32)
+    relac = np.zeros(m, np.float64)
+    L.degree_dist(_p(deg, _P_I32), _p(dist, _P_I32), n)
+    L.degree_dist_rel(_p(dist, _P_I32), rel.ctypes.data_as(POINTER(c_double)), m, n)
+    L.degree_dist_ac(_p(dist, _P_I32), rel.ctypes.data_as(POINTER(c_double)), _p(ac, _P_I32),
+                     relac.ctypes.data_as(POINTER(c_double)), m)
+    idx = [0, 1] + [1 << j for j in range(1, 40) if (1 << j) < m]
+    return {"max": m, "argmax": ix.value, "mean": mean.value, "sd": sd.value,
+            "dist_ac": ac[idx].astype(np.int64), "dist_rel_ac": relac[idx]}
 
 
 def ref_available() -> bool:
@@ -227,3 +298,95 @@ def ref_seq_cooc(I, J, n, r):
     with _quiet_stdout():
         L.bfs_seq_td_cooc(_p(I, _P_I32), _p(J, _P_I32), _p(sg, _P_F32), r, I.shape[0], n)
     return sg
+
+
+# ------------------------------------- the reference's own GPU kernels
+
+_refgpu = None
+
+
+def refgpu_available() -> bool:
+    """True when librefgpu.so and at least one of the reference's kernel
+    images (oracle/_ref/*.cubin, built where the reference tree is) exist and
+    a GPU is visible."""
+    return _refgpu_lib() is not None and _refgpu_mask() != 0
+
+
+def _refgpu_lib():
+    global _refgpu
+    if _refgpu is None:
+        path = HERE / "librefgpu.so"
+        if not path.exists():
+            return None
+        L = ctypes.CDLL(str(path))
+        L.refgpu_load.argtypes = [ctypes.c_char_p]
+        L.refgpu_last_error.restype = ctypes.c_char_p
+        P = ctypes.POINTER(c_double)
+        L.refgpu_td_csc_sc.argtypes = [_P_I32, _P_I32, _P_I32, _P_F32, c_int, c_int, c_int, P, _P_I32]
+        L.refgpu_bu_csc_sc.argtypes = [_P_I32, _P_I32, _P_I32, c_int, c_int, c_int, c_int, P, _P_I32]
+        L.refgpu_tdbu_csc_sc.argtypes = [_P_I32, _P_I32, _P_I32, _P_I32, c_int, c_int, c_int, c_int,
+                                         P, _P_I32, _P_I32]
+        L.refgpu_td_cooc_sc.argtypes = [_P_I32, _P_I32, _P_F32, c_int, c_int, c_int, P, _P_I32]
+        _refgpu = L
+    return _refgpu
+
+
+def _refgpu_mask() -> int:
+    L = _refgpu_lib()
+    return 0 if L is None else int(L.refgpu_load(str(REF_DIR).encode()))
+
+
+def _refgpu_call(name, *args):
+    L = _refgpu_lib()
+    if L is None or _refgpu_mask() == 0:
+        raise RuntimeError("reference GPU kernel images not available")
+    rc = getattr(L, name)(*args)
+    if rc != 0:
+        raise RuntimeError(f"{name}: {L.refgpu_last_error().decode()}")
+
+
+def refgpu_tdbu_csc_sc(cp, ic, r, bbreak=1):
+    """The reference's bfs_gpu_tdbu_csc_sc kernels on this GPU: (S, int32
+    sigma, kernel ms, top-down levels, bottom-up levels)."""
+    cp, ic = _i32(cp), _i32(ic)
+    n = cp.shape[0] - 1
+    S = np.zeros(n, np.int32)
+    sg = np.zeros(n, np.int32)
+    ms, td, bu = c_double(), np.zeros(1, np.int32), np.zeros(1, np.int32)
+    _refgpu_call("refgpu_tdbu_csc_sc", _p(ic, _P_I32), _p(cp, _P_I32), _p(S, _P_I32),
+                 _p(sg, _P_I32), int(r), ic.shape[0], n, int(bbreak), ctypes.byref(ms),
+                 _p(td, _P_I32), _p(bu, _P_I32))
+    return S, sg, ms.value, int(td[0]), int(bu[0])
+
+
+def refgpu_td_csc_sc(cp, ic, r):
+    """The reference's bfs_gpu_td_csc_sc kernels: (S, float sigma, ms, levels)."""
+    cp, ic = _i32(cp), _i32(ic)
+    n = cp.shape[0] - 1
+    S = np.zeros(n, np.int32)
+    sg = np.zeros(n, np.float32)
+    ms, lv = c_double(), np.zeros(1, np.int32)
+    _refgpu_call("refgpu_td_csc_sc", _p(ic, _P_I32), _p(cp, _P_I32), _p(S, _P_I32),
+                 _p(sg, _P_F32), int(r), ic.shape[0], n, ctypes.byref(ms), _p(lv, _P_I32))
+    return S, sg, ms.value, int(lv[0])
+
+
+def refgpu_bu_csc_sc(cp, ic, r, bbreak=1):
+    """The reference's bfs_gpu_bu_csc_sc kernel: (S, ms, levels)."""
+    cp, ic = _i32(cp), _i32(ic)
+    n = cp.shape[0] - 1
+    S = np.zeros(n, np.int32)
+    ms, lv = c_double(), np.zeros(1, np.int32)
+    _refgpu_call("refgpu_bu_csc_sc", _p(ic, _P_I32), _p(cp, _P_I32), _p(S, _P_I32), int(r),
+                 ic.shape[0], n, int(bbreak), ctypes.byref(ms), _p(lv, _P_I32))
+    return S, ms.value, int(lv[0])
+
+
+def refgpu_td_cooc_sc(I, J, n, r):
+    """The reference's bfs_gpu_td_cooc_sc kernels: (float sigma, ms, levels)."""
+    I, J = _i32(I), _i32(J)
+    sg = np.zeros(n, np.float32)
+    ms, lv = c_double(), np.zeros(1, np.int32)
+    _refgpu_call("refgpu_td_cooc_sc", _p(I, _P_I32), _p(J, _P_I32), _p(sg, _P_F32), int(r),
+                 I.shape[0], n, ctypes.byref(ms), _p(lv, _P_I32))
+    return sg, ms.value, int(lv[0])

@@ -14,6 +14,7 @@
 #define _GNU_SOURCE
 #include "tbfs_oracle.h"
 
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -589,4 +590,58 @@ int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int 
   free(q);
   free(delta);
   return ovf_roots;
+}
+
+/* ------------------------------------------------------ degree statistics */
+
+/* degree_max (TurboBFS_CSC_TD/degree.c:36-48): strict '>' keeps the first
+ * vertex of the maximum.  degree_sta (:54-76): mean = sum / n; variance =
+ * sum of pow(deg - mean, 2) in vertex order / (n - 1).  degree_dist,
+ * degree_dist_rel, degree_dist_ac (:83-141): per-degree counts, percentages
+ * 100 * count / n, then buckets 0 and 1 copied and every later bucket
+ * [low, 2 low) summed in degree order into entry `low` while low < max. */
+int oracle_degree_stats(const int *deg, int n, int64_t *maxd, int64_t *argmax, double *mean,
+                        double *sd, int64_t *dist_ac, double *dist_rel_ac, int cap) {
+  int64_t mx = 0, ix = -1, sum = 0;
+  for (int i = 0; i < n; ++i) {
+    if (deg[i] > mx) {
+      mx = deg[i];
+      ix = i;
+    }
+    sum += deg[i];
+  }
+  const double m = n ? (double)sum / (double)n : 0.0;
+  double ss = 0.0;
+  for (int i = 0; i < n; ++i) ss += pow((double)deg[i] - m, 2);
+  *maxd = mx;
+  *argmax = ix;
+  *mean = m;
+  *sd = sqrt(ss / (double)(n - 1));
+  int need = 2;
+  for (int64_t low = 2; low < mx; low *= 2) ++need;
+  if (cap < need) return -1;
+  int64_t *dist = (int64_t *)calloc((size_t)mx + 1, sizeof(int64_t));
+  double *rel = (double *)calloc((size_t)mx + 1, sizeof(double));
+  if (!dist || !rel) {
+    free(dist);
+    free(rel);
+    return -1;
+  }
+  for (int i = 0; i < n; ++i) dist[deg[i]]++;
+  for (int64_t d = 0; d <= mx; ++d) rel[d] = (double)dist[d] * 100.0 / ((double)n);
+  memset(dist_ac, 0, (size_t)cap * sizeof(int64_t));
+  memset(dist_rel_ac, 0, (size_t)cap * sizeof(double));
+  for (int b = 0; b < 2 && b <= mx; ++b) {
+    dist_ac[b] = dist[b];
+    dist_rel_ac[b] = rel[b];
+  }
+  int b = 2;
+  for (int64_t low = 2; low < mx; low *= 2, ++b)
+    for (int64_t d = low; d < 2 * low && d <= mx; ++d) {
+      dist_ac[b] += dist[d];
+      dist_rel_ac[b] += rel[d];
+    }
+  free(dist);
+  free(rel);
+  return 0;
 }

@@ -75,6 +75,22 @@ double oracle_seq_many(const int *IC, const int *CP, int nz, int n,
 /* Brandes betweenness with the GPU sweep's summation order (see .c) */
 int oracle_brandes(const int *orp, const int *ojr, int n, const int *roots, int k, double *bc);
 
+/* Degree statistics of a degree vector deg[n], as the reference's drivers
+ * compute them (TurboBFS_CSC_TD/degree.c:36-141, called from
+ * bfstdcsc_main.c:177-195): the maximum and the first vertex holding it
+ * (*argmax = -1 when every degree is 0; the reference leaves it unset), the
+ * mean (sum in int64 here; the reference's int sum wraps past 2^31) and the
+ * sample standard deviation (divisor n - 1), and the accumulated log2
+ * distribution: dist_ac[0] / dist_ac[1] = vertices of degree 0 / 1 and
+ * dist_ac[b] (b >= 2) = vertices with degree in [2^(b-1), 2^b) while
+ * 2^(b-1) < max -- so a maximum that is a power of two is counted in no
+ * bucket, as in degree_dist_ac -- with dist_rel_ac the same sums of the
+ * per-degree percentages 100 * count / n.  cap = entries of dist_ac and
+ * dist_rel_ac (unused buckets are 0).  Returns 0, or -1 when cap is too
+ * small for max. */
+int oracle_degree_stats(const int *deg, int n, int64_t *maxd, int64_t *argmax, double *mean,
+                        double *sd, int64_t *dist_ac, double *dist_rel_ac, int cap);
+
 #ifdef __cplusplus
 }
 #endif

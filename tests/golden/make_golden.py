@@ -1,9 +1,9 @@
 """Regenerate the golden vectors in tests/golden/*.npz.
 
-Run in a container that has the reference tree (default /root/reference, or
-$TBFS_REFERENCE) after `make -C oracle ref`:
+Run on a machine that has the reference tree, after
+`make -C oracle ref REF=<tree>`:
 
-    python tests/golden/make_golden.py
+    TBFS_REFERENCE=<tree> python tests/golden/make_golden.py
 
 For every reference fixture (graphData/*.mtx, loaded with the reference's
 own CSC construction and the `ug` flag its run scripts use) and for a few
@@ -33,7 +33,9 @@ import oracle  # noqa: E402
 from turbobfs_gb300 import graphs  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-REF = Path(os.environ.get("TBFS_REFERENCE", "/root/reference"))
+if not os.environ.get("TBFS_REFERENCE"):
+    sys.exit("make_golden.py: set TBFS_REFERENCE to the reference tree")
+REF = Path(os.environ["TBFS_REFERENCE"])
 
 # (name, ug, roots); roots follow the run scripts (TurboBFS_CSC_TD/run_bfstdcsc.sh:10-37)
 FIXTURES = [

@@ -10,7 +10,8 @@ import pytest
 from golden_data import REFERENCE_FIXTURES, load
 from turbobfs_gb300 import graphs
 
-REF = Path(os.environ.get("TBFS_REFERENCE", "/root/reference"))
+# the reference tree (its graphData/ fixtures), where this machine has one
+REF = Path(os.environ["TBFS_REFERENCE"]) if os.environ.get("TBFS_REFERENCE") else None
 
 
 def _digest(g):
@@ -118,7 +119,8 @@ def test_components_and_roots():
     assert prof["hist_log2"].sum() == g.n and prof["max"] == g.degrees().max()
 
 
-@pytest.mark.skipif(not (REF / "graphData").is_dir(), reason="reference fixtures not present")
+@pytest.mark.skipif(REF is None or not (REF / "graphData").is_dir(),
+                    reason="TBFS_REFERENCE unset or without graphData/")
 @pytest.mark.parametrize("name", REFERENCE_FIXTURES)
 def test_mm_loader_matches_golden(name):
     fx = load(name)

@@ -69,6 +69,31 @@ def test_noalloc_directed_out_lists_and_depth_only(gpu_available):
             assert rc == 0 and np.array_equal(S, ref.S)
 
 
+def test_noalloc_allocates_nothing(gpu_available):
+    """After a warm-up call, further calls leave the device's free memory
+    unchanged (outputs preallocated and reused, torch's allocator idle)."""
+    torch = pytest.importorskip("torch")
+    h = graphs.rmat(14, 16, seed=7)
+    cp = torch.from_numpy(h.col_ptr).cuda()
+    ic = torch.from_numpy(h.row_idx).cuda()
+    S = torch.empty(h.n, dtype=torch.int32, device="cuda")
+    sg = torch.empty(h.n, dtype=torch.int64, device="cuda")
+    st = _lib.Stats()
+
+    def call(r):
+        return tb.lib().tbfs_bfs_noalloc(cp.data_ptr(), ic.data_ptr(), None, None, h.n, h.nnz,
+                                         int(r), 0, S.data_ptr(), sg.data_ptr(), None,
+                                         ctypes.byref(st))
+
+    assert call(0) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for r in graphs.pick_roots(h, 4, seed=7):
+        assert call(r) == 0, tb.lib().tbfs_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_rejects_too_large_and_bad_input(gpu_available):
     torch = pytest.importorskip("torch")
     n = MAX_N + 1

@@ -64,6 +64,42 @@ class Stats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+DEGREE_IN, DEGREE_OUT, DEGREE_UNDIRECTED = 0, 1, 2
+DEGREE_BUCKETS = 40
+
+
+class DegreeStats(ctypes.Structure):
+    _fields_ = [
+        ("max_degree", c_int64),
+        ("argmax", c_int64),
+        ("sum", c_int64),
+        ("mean", c_double),
+        ("sd", c_double),
+        ("dist_ac", c_int64 * DEGREE_BUCKETS),
+        ("dist_rel_ac", c_double * DEGREE_BUCKETS),
+    ]
+
+
+class Validation(ctypes.Structure):
+    _fields_ = [
+        ("bad_root", c_int64),
+        ("bad_depth", c_int64),
+        ("skips_level", c_int64),
+        ("no_parent", c_int64),
+        ("sigma_mismatch", c_int64),
+        ("first_bad", c_int64),
+        ("visited", c_int64),
+        ("edges", c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: int(getattr(self, name)) for name, _ in self._fields_}
+
+    def ok(self) -> bool:
+        return (self.bad_root == 0 and self.bad_depth == 0 and self.skips_level == 0
+                and self.no_parent == 0 and self.sigma_mismatch == 0)
+
+
 class HostCSCStruct(ctypes.Structure):
     _fields_ = [
         ("n", c_int32),
@@ -86,12 +122,15 @@ _SIGNATURES = {
     "tbfs_graph_destroy": (None, [c_void_p]),
     "tbfs_graph_info": (c_int, [c_void_p, _P_I32, _P_I64, POINTER(c_uint32)]),
     "tbfs_bfs": (c_int, [c_void_p, c_int32, POINTER(Options), _P_I32, _P_I64, POINTER(Stats)]),
+    "tbfs_bfs_validate": (c_int, [c_void_p, c_int32, c_void_p, c_void_p, c_int32, c_void_p,
+                                  POINTER(Validation)]),
     "tbfs_graph_last_stats": (c_int, [c_void_p, POINTER(Stats)]),
     "tbfs_bfs_many": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), _P_I32, _P_I64,
                               POINTER(Stats)]),
     "tbfs_bfs_batch": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_int32, c_void_p,
                                c_void_p, POINTER(Stats)]),
     "tbfs_graph_degree_profile": (c_int, [c_void_p, _P_I64, _P_I64, POINTER(c_double)]),
+    "tbfs_graph_degree_stats": (c_int, [c_void_p, c_int32, POINTER(DegreeStats), _P_I64, c_int64]),
     "tbfs_graph_create_edges": (c_int, [_P_I32, _P_I32, c_int32, c_int64, c_uint32, c_uint32,
                                         POINTER(c_void_p)]),
     "tbfs_graph_create_mm": (c_int, [c_char_p, c_int64, c_int32, c_uint32, c_uint32,

@@ -19,7 +19,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from ._lib import (GRAPH_KEEP_ORDER, GRAPH_SYMMETRIC, LAYOUT_ROOT_MAJOR, LAYOUT_VERTEX_MAJOR,
-                   Options, Stats, check, lib)
+                   DegreeStats, Options, Stats, Validation, check, lib)
 
 MODES = {"auto": 0, "do": 0, "td": 1, "top_down": 1, "bu": 2, "bottom_up": 2}
 _P_I32 = ctypes.POINTER(ctypes.c_int32)
@@ -254,6 +254,54 @@ class Graph:
         check(lib().tbfs_graph_degree_profile(self.handle, _ptr(h, _P_I64), ctypes.byref(mx),
                                               ctypes.byref(mean)), "tbfs_graph_degree_profile")
         return {"hist": h, "max": int(mx.value), "mean": float(mean.value)}
+
+    def validate(self, root: int, S, sigma=None) -> dict:
+        """Check a BFS result (S int32[n], sigma int64[n] or None; numpy
+        arrays, or torch CUDA tensors) against this graph on the device
+        (tbfs_bfs_validate): violation counts by kind, 'first_bad', the
+        reached vertices and their in-list entries, and 'ok'."""
+        v = Validation()
+        on_dev = hasattr(S, "data_ptr")
+        if on_dev:
+            s_ptr = S.data_ptr()
+            g_ptr = sigma.data_ptr() if sigma is not None else None
+        else:
+            S = _i32(S)
+            s_ptr = S.ctypes.data
+            if sigma is not None:
+                sigma = np.ascontiguousarray(sigma, dtype=np.int64)
+            g_ptr = sigma.ctypes.data if sigma is not None else None
+        check(lib().tbfs_bfs_validate(self.handle, int(root), s_ptr, g_ptr, 1 if on_dev else 0,
+                                      None, ctypes.byref(v)), "tbfs_bfs_validate")
+        out = v.as_dict()
+        out["ok"] = v.ok()
+        return out
+
+    def degree_stats(self, kind: str = "undirected", full: bool = False) -> dict:
+        """The reference driver's degree statistics (TurboBFS_CSC_TD/degree.c:22-141),
+        computed on the device: {'max', 'argmax', 'sum', 'mean', 'sd',
+        'dist_ac' int64[b], 'dist_rel_ac' float64[b]} with b the buckets in
+        use (degree 0, 1, then [2^(j-1), 2^j) for 2^(j-1) < max), and with
+        full=True 'dist' int64[max+1] (vertices per degree).  kind: 'in',
+        'out' or 'undirected' (degree_ug: out + in of the entries)."""
+        kinds = {"in": 0, "out": 1, "undirected": 2}
+        st = DegreeStats()
+        check(lib().tbfs_graph_degree_stats(self.handle, kinds[kind], ctypes.byref(st), None, 0),
+              "tbfs_graph_degree_stats")
+        nb = 2
+        while nb < 40 and (1 << (nb - 1)) < st.max_degree:
+            nb += 1
+        out = {"max": int(st.max_degree), "argmax": int(st.argmax), "sum": int(st.sum),
+               "mean": float(st.mean), "sd": float(st.sd),
+               "dist_ac": np.array(st.dist_ac[:nb], dtype=np.int64),
+               "dist_rel_ac": np.array(st.dist_rel_ac[:nb], dtype=np.float64)}
+        if full:
+            dist = np.zeros(st.max_degree + 1, dtype=np.int64)
+            check(lib().tbfs_graph_degree_stats(self.handle, kinds[kind], ctypes.byref(st),
+                                                _ptr(dist, _P_I64), dist.shape[0]),
+                  "tbfs_graph_degree_stats")
+            out["dist"] = dist
+        return out
 
     def autotune(self, roots, cache: str | None = None, **kw) -> dict:
         """Tuned {'alpha', 'beta', 'pull_ratio', 'from_cache'} for this graph

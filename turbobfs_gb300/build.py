@@ -23,7 +23,7 @@ LIB = PKG / "libtbfs.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["bfs_engine.cu", "batch_engine.cu", "multi_engine.cu", "graph_ingest.cu", "api.cu",
               "batch_api.cu", "multi_api.cu", "brandes.cu", "tune.cu",
-              "noalloc.cu", "mm_ingest.cu", "devmem.cu"]
+              "noalloc.cu", "mm_ingest.cu", "devmem.cu", "validate.cu"]
 C_SOURCES = ["host_graph.c"]
 
 
@@ -104,13 +104,17 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
 
 
 def build_oracle(verbose: bool = False) -> Path:
-    """Build the CPU checker (oracle/liboracle.so) and, when the reference tree
-    is present on this machine, the reference's own sequential sources."""
+    """Build the checker: the CPU restatement (oracle/liboracle.so), the host
+    driver of the reference's GPU kernel images (oracle/librefgpu.so) and, when
+    the reference tree is present on this machine, the reference's own
+    sequential sources and GPU kernel images (oracle/_ref/)."""
     odir = ROOT / "oracle"
-    _run(["make", "-C", str(odir), "liboracle.so"], verbose)
-    ref = Path(os.environ.get("TBFS_REFERENCE", "/root/reference"))
+    _run(["make", "-C", str(odir), "liboracle.so", "librefgpu.so", f"NVCC={nvcc_path()}"], verbose)
+    # the reference tree: $TBFS_REFERENCE, else where the build container
+    # mounts it; absent on other machines, which then use prebuilt files only
+    ref = Path(os.environ.get("TBFS_REFERENCE") or "/root/reference")
     if (ref / "TurboBFS_CSC_TD").is_dir():
-        _run(["make", "-C", str(odir), "ref", f"REF={ref}"], verbose)
+        _run(["make", "-C", str(odir), "ref", f"REF={ref}", f"NVCC={nvcc_path()}"], verbose)
     return odir / "liboracle.so"
 
 

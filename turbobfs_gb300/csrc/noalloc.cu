@@ -10,16 +10,25 @@
  * graph and the outputs as device pointers; the frontier queues and the
  * control block the traversal needs live in one file-scope device array,
  * g_noalloc_scratch, sized for graphs of up to TBFS_NOALLOC_MAX_VERTICES
- * vertices.  That array is part of the library image: every GPU that loads
- * the library holds it (about 36 MB) until the process exits.
+ * vertices.  That array is part of the library's device code: once that code
+ * is loaded on a GPU, the GPU holds the array (about 36 MB) until the process
+ * exits.
  *
  * Host code cannot use the array's name as a device address; on the first
  * call on each device (with that device current) the address is looked up
- * once with cudaGetSymbolAddress and cached.  Do that first call before any
- * stream capture.  Every call shares the one array: the control block is
- * cleared at the start of each call, and two calls whose work overlaps on
- * the GPU (different streams or host threads without ordering) race on it.
+ * with cudaGetSymbolAddress and cached for the device's current context.
+ * CUDA loads device code lazily, so when nothing else of the library ran on
+ * that device yet, this first call is also the moment the 36 MB are
+ * committed: make it as a warm-up before the host framework reserves the
+ * device memory it manages, and before any stream capture.  If the memory
+ * is not there, the call fails with TBFS_ERR_OUT_OF_MEMORY.  A new context
+ * on the device (after cudaDeviceReset) gets a fresh lookup.  Every call
+ * waits for its traversal to finish on the caller's stream.  Every call
+ * shares the one array: the control block is cleared at the start of each
+ * call, and two calls whose work overlaps on the GPU (different streams or
+ * host threads without ordering) race on it.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -42,6 +51,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 struct DeviceSetup {
   bool ready = false;
+  unsigned long long ctx_id = 0;    /* context the address belongs to */
   unsigned char *scratch = nullptr; /* device address of g_noalloc_scratch */
   tbfs::LaunchGeom geom;
 };
@@ -60,18 +70,53 @@ tbfs_status cuda_fail(cudaError_t e, const char *what) {
   return TBFS_ERR_CUDA;
 }
 
-/* once per device, with that device current */
+/* identifier of the calling thread's current context (driver entry points
+ * fetched through the runtime, so the library needs no libcuda at link time);
+ * 0 if unavailable */
+unsigned long long current_context_id() {
+  static CUresult (*get_current)(CUcontext *) = nullptr;
+  static CUresult (*get_id)(CUcontext, unsigned long long *) = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void *f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CUresult (*)(CUcontext *)>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CUresult (*)(CUcontext, unsigned long long *)>(f);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx &&
+      get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+/* once per device and context, with that device current */
 tbfs_status setup_device(int dev, DeviceSetup **out) {
   if (dev < 0 || dev >= kMaxDevices) return fail(TBFS_ERR_UNSUPPORTED, "device index too large");
+  /* 0 when this thread has no current context yet: the lookup below makes
+   * the device's primary context current */
+  unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_setup_mu);
   DeviceSetup &s = g_setup[dev];
-  if (!s.ready) {
+  if (!s.ready || ctx == 0 || s.ctx_id != ctx) {
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e == cudaErrorMemoryAllocation)
+      return fail(TBFS_ERR_OUT_OF_MEMORY,
+                  "tbfs_bfs_noalloc: loading the library's device code (with its 36 MB scratch "
+                  "array) on this device failed for lack of memory; make the first call before "
+                  "device memory is reserved by the host framework");
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(scratch)");
     e = tbfs::bfs_geometry(dev, &s.geom);
     if (e != cudaSuccess) return cuda_fail(e, "launch geometry");
     s.scratch = static_cast<unsigned char *>(ptr);
+    s.ctx_id = current_context_id();
     s.ready = true;
   }
   *out = &s;
@@ -125,7 +170,7 @@ extern "C" tbfs_status tbfs_bfs_noalloc(const int32_t *d_col_ptr, const int32_t 
     return cuda_fail(e, "read validation flag");
   if (hflag) return fail(TBFS_ERR_INVALID_ARG, "tbfs_bfs_noalloc: malformed CSC input");
 
-  tbfs::BfsParams p;
+  tbfs::BfsParams p = {};
   p.cp = d_col_ptr;
   p.ic = d_row_idx;
   p.rp = rp;

@@ -3,9 +3,20 @@
  * autotuner of the traversal parameters keyed by it.
  *
  * Degree profile: hist[b] = vertices whose in-degree d has floor(log2(d+1))
- * == b (b < 40), the maximum and the mean -- the statistics the reference
- * prints from its host code (TurboBFS_CSC_TD/degree.c:22-141), computed
- * here by one pass over col_ptr with block-aggregated histograms.
+ * == b (b < 40), the maximum and the mean, by one pass over col_ptr with
+ * block-aggregated histograms: the key of the autotuner's cache.
+ *
+ * Degree statistics (tbfs_graph_degree_stats): what the reference's drivers
+ * print from TurboBFS_CSC_TD/degree.c:22-141 -- the degree vector
+ * (degree_ug: out + in of the file entries; in- or out-degree alone),
+ * its maximum and the first vertex holding it (degree_max), mean and sample
+ * standard deviation (degree_sta), and the per-degree and accumulated log2
+ * distributions with their percentages (degree_dist, degree_dist_rel,
+ * degree_dist_ac).  The device makes two passes over the lists' pointers:
+ * maximum and sum, then the per-degree histogram (shared-memory counters for
+ * small degrees) and the first vertex of maximum degree in the caller's
+ * numbering.  The host finishes from the histogram in degree order, so the
+ * accumulated distributions are the reference's to the bit.
  *
  * Autotuner: the direction switch (alpha, beta) and the path-count schedule
  * (pull_ratio) of the single-source engine are chosen by timing traversals
@@ -52,6 +63,71 @@ __global__ void degree_profile_kernel(const int *cp, int n, unsigned long long *
   __syncthreads();
   if (threadIdx.x < kBuckets && h[threadIdx.x]) atomicAdd(hist + threadIdx.x, (unsigned long long)h[threadIdx.x]);
   if (threadIdx.x == 0) atomicMax(maxdeg, mx);
+}
+
+/* degree of internal vertex v: in (cp), out (rp), or the undirected degree
+ * (in-list length of a symmetric graph, in + out otherwise) */
+__device__ __forceinline__ int vertex_degree(const int *cp, const int *rp, int kind, bool sym,
+                                             int v) {
+  const int din = __ldg(cp + v + 1) - __ldg(cp + v);
+  if (kind == TBFS_DEGREE_IN || (kind == TBFS_DEGREE_UNDIRECTED && sym)) return din;
+  const int dout = __ldg(rp + v + 1) - __ldg(rp + v);
+  return kind == TBFS_DEGREE_OUT ? dout : din + dout;
+}
+
+/* pass 1: maximum and sum of the degrees */
+__global__ void degree_max_sum_kernel(const int *cp, const int *rp, int kind, bool sym, int n,
+                                      unsigned long long *sum, int *maxdeg) {
+  __shared__ unsigned long long s_sum;
+  __shared__ int s_max;
+  if (threadIdx.x == 0) {
+    s_sum = 0;
+    s_max = 0;
+  }
+  __syncthreads();
+  unsigned long long ls = 0;
+  int lm = 0;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int d = vertex_degree(cp, rp, kind, sym, (int)v);
+    ls += (unsigned long long)d;
+    lm = max(lm, d);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ls += __shfl_xor_sync(0xffffffffu, ls, o);
+    lm = max(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_sum, ls);
+    atomicMax(&s_max, lm);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(sum, s_sum);
+    atomicMax(maxdeg, s_max);
+  }
+}
+
+/* pass 2: hist[d] = vertices of degree d (d <= maxd), counted in shared
+ * memory below kSmallDeg; *argmax = smallest caller id of maximum degree */
+constexpr int kSmallDeg = 2048;
+__global__ void degree_hist_kernel(const int *cp, const int *rp, int kind, bool sym, int n,
+                                   const int *perm, int maxd, unsigned long long *hist,
+                                   int *argmax) {
+  __shared__ unsigned h[kSmallDeg];
+  for (int i = threadIdx.x; i < kSmallDeg; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int d = vertex_degree(cp, rp, kind, sym, (int)v);
+    if (d < kSmallDeg) atomicAdd(&h[d], 1u);
+    else atomicAdd(hist + d, 1ull);
+    if (d == maxd) atomicMin(argmax, perm ? __ldg(perm + v) : (int)v);
+  }
+  __syncthreads();
+  const int lim = maxd + 1 < kSmallDeg ? maxd + 1 : kSmallDeg;
+  for (int i = threadIdx.x; i < lim; i += blockDim.x)
+    if (h[i]) atomicAdd(hist + i, (unsigned long long)h[i]);
 }
 
 std::mutex g_cache_mu;
@@ -128,6 +204,82 @@ extern "C" tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40,
   for (int b = 0; b < tbfs::kBuckets; ++b) hist40[b] = (int64_t)h[b];
   if (max_degree) *max_degree = mx;
   if (mean_degree) *mean_degree = g->n ? (double)g->nnz / (double)g->n : 0.0;
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_graph_degree_stats(tbfs_graph *g, int32_t kind,
+                                               tbfs_degree_stats *out, int64_t *dist,
+                                               int64_t dist_cap) {
+  if (!g || !out || kind < TBFS_DEGREE_IN || kind > TBFS_DEGREE_UNDIRECTED ||
+      (dist && dist_cap < 0)) {
+    tbfs_set_error("tbfs_graph_degree_stats: null graph or output, or unknown degree kind");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  memset(out, 0, sizeof *out);
+  out->argmax = -1;
+  const int n = g->n;
+  if (n == 0) return TBFS_OK;
+  const bool sym = !g->separate_out;
+  const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, 1216);
+  cudaError_t e = cudaSetDevice(g->device);
+  unsigned long long *dsum = nullptr, *hist = nullptr;
+  int *dmax = nullptr;
+  unsigned long long hsum = 0;
+  int hmax = 0, harg = -1;
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&dsum, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    dmax = reinterpret_cast<int *>(dsum + 1);
+    e = cudaMemset(dsum, 0, 2 * sizeof(unsigned long long));
+  }
+  if (e == cudaSuccess) {
+    tbfs::degree_max_sum_kernel<<<blocks, 256>>>(g->cp, g->rp, kind, sym, n, dsum, dmax);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&hsum, dsum, sizeof hsum, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&hmax, dmax, sizeof hmax, cudaMemcpyDeviceToHost);
+  /* histogram of hmax + 1 counters, then the argmax word */
+  const size_t hbytes = ((size_t)hmax + 1) * sizeof(unsigned long long);
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&hist, hbytes + sizeof(unsigned long long));
+  int *darg = hist ? reinterpret_cast<int *>(reinterpret_cast<char *>(hist) + hbytes) : nullptr;
+  if (e == cudaSuccess) e = cudaMemset(hist, 0, hbytes);
+  if (e == cudaSuccess) e = cudaMemset(darg, 0x7f, sizeof(int));
+  if (e == cudaSuccess) {
+    tbfs::degree_hist_kernel<<<blocks, 256>>>(g->cp, g->rp, kind, sym, n, g->perm, hmax, hist,
+                                               darg);
+    e = cudaGetLastError();
+  }
+  std::vector<unsigned long long> h((size_t)hmax + 1);
+  if (e == cudaSuccess) e = cudaMemcpy(h.data(), hist, hbytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&harg, darg, sizeof harg, cudaMemcpyDeviceToHost);
+  tbfs::dev_free(hist);
+  tbfs::dev_free(dsum);
+  if (e != cudaSuccess) {
+    tbfs_set_error("tbfs_graph_degree_stats: %s", cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? TBFS_ERR_OUT_OF_MEMORY : TBFS_ERR_CUDA;
+  }
+  /* host side, in degree order as degree.c:54-141 */
+  out->max_degree = hmax;
+  out->argmax = hmax > 0 ? harg : -1;
+  out->sum = (int64_t)hsum;
+  out->mean = (double)hsum / (double)n;
+  double ss = 0.0;
+  for (int d = 0; d <= hmax; ++d)
+    if (h[(size_t)d]) ss += (double)h[(size_t)d] * std::pow((double)d - out->mean, 2);
+  out->sd = std::sqrt(ss / (double)(n - 1));
+  std::vector<double> rel((size_t)hmax + 1);
+  for (int d = 0; d <= hmax; ++d) rel[(size_t)d] = (double)h[(size_t)d] * 100.0 / ((double)n);
+  for (int b = 0; b < 2 && b <= hmax; ++b) {
+    out->dist_ac[b] = (int64_t)h[(size_t)b];
+    out->dist_rel_ac[b] = rel[(size_t)b];
+  }
+  int b = 2;
+  for (long long low = 2; low < hmax && b < TBFS_DEGREE_BUCKETS; low *= 2, ++b)
+    for (long long d = low; d < 2 * low && d <= hmax; ++d) {
+      out->dist_ac[b] += (int64_t)h[(size_t)d];
+      out->dist_rel_ac[b] += rel[(size_t)d];
+    }
+  if (dist)
+    for (int64_t d = 0; d < dist_cap && d <= hmax; ++d) dist[d] = (int64_t)h[(size_t)d];
   return TBFS_OK;
 }
 
