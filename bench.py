@@ -80,7 +80,7 @@ def parse_args(argv=None):
     p.add_argument("--serving-max-scale", type=int, default=24)
     p.add_argument("--serving-max-side", type=int, default=4096)
     p.add_argument("--serving-rates", default="100,400,1600")
-    p.add_argument("--serving-queries", type=int, default=300)
+    p.add_argument("--serving-queries", type=int, default=2000)
     return p.parse_args(argv)
 
 
@@ -337,7 +337,7 @@ def run_tbfs(args, world, rank, local):
     if not args.no_autotune and args.mode == "auto":
         # the library's autotuner, timed on 8 of the roots (not cached)
         tu = g.autotune(roots[:8])
-        kw = {"alpha": tu["alpha"], "beta": tu["beta"], "pull_ratio": tu["pull_ratio"]}
+        kw = {k: v for k, v in tu.items() if k != "from_cache"}
         tuning = {"autotuned": True, "sample_roots": 8, **kw}
     o = make_options(args.mode, True, outputs_on_device=True, **kw)
     stats = (_lib.Stats * k)()
@@ -522,6 +522,7 @@ def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
         o = make_options("auto", True)
         o.alpha, o.beta, o.mode = o_dev.alpha, o_dev.beta, o_dev.mode
         o.pull_ratio = o_dev.pull_ratio
+        o.max_ept, o.ctas_per_sm = o_dev.max_ept, o_dev.ctas_per_sm
         stats = (_lib.Stats * k)()
 
         split = {"create_ms": 0.0, "traverse_and_copy_ms": 0.0, "destroy_ms": 0.0}
@@ -655,7 +656,10 @@ def batched_report(args):
         t_batch = _event_ms(batch)
         same = bool(torch.equal(S[::37], S_ref) and torch.equal(sg[::37], sg_ref))
         edges = sum(st[i].edges for i in range(k)) / 2
-        alg = sum(4 * st[i].edges + 8 * st[i].visited + 12 * n for i in range(k))
+        per_root = sum(4 * st[i].edges + 8 * st[i].visited + 12 * n for i in range(k))
+        # the batch's own mandatory bytes: every root's S and sigma written once
+        # (12 k n) and one pass over the lists and their pointers
+        batch_bytes = 12 * k * n + 4 * h.nnz + 8 * n
         peak, peak_kind = measured_peak()
         out["frontier_matrix"] = {
             "workload": f"RMAT scale {args.batch_scale}, edgefactor 16, {k} roots in one launch, "
@@ -666,12 +670,17 @@ def batched_report(args):
             "speedup_vs_plain": t_plain / t_batch,
             "launches": {"batched": (k + 255) // 256, "plain": k},
             "results_identical_to_plain": same,
-            "roofline": {"bound": "hbm", "algorithmic_bytes": alg,
-                         "achieved_gbs": alg / (t_batch / 1e3) / 1e9,
-                         "frac": alg / (t_batch / 1e3) / 1e9 / peak,
+            "roofline": {"bound": "hbm", "algorithmic_bytes": batch_bytes,
+                         "achieved_gbs": batch_bytes / (t_batch / 1e3) / 1e9,
+                         "frac": batch_bytes / (t_batch / 1e3) / 1e9 / peak,
                          "peak": peak, "peak_source": f"{peak_kind} hbm_gbs",
-                         "note": "sum over roots of 4 nnz_c + 8 n_c + 12 n (per-root bytes; the "
-                                 "batch shares list reads, so this can exceed 1)"},
+                         "note": "the batch's own bytes: 12 k n of S and sigma written once plus "
+                                 "one pass over col_ptr / row_idx; the kernels' measured DRAM "
+                                 "traffic is in profiles/launches_batched_report.md"},
+            "per_root_bytes": {"bytes": per_root,
+                               "gbs": per_root / (t_batch / 1e3) / 1e9,
+                               "note": "sum over roots of 4 nnz_c + 8 n_c + 12 n, what k "
+                                       "single-source traversals would read and write"},
         }
         o2 = make_options("auto", False, outputs_on_device=True)
 
@@ -776,6 +785,42 @@ def serving_graph_set(count, max_scale, max_side):
     return hs
 
 
+def plain_fifo(gs, qg, qr, arrivals):
+    """One-at-a-time serving on the same arrivals: a worker thread takes the
+    queries in arrival order and runs each with tbfs_bfs (results to host
+    memory) once it has arrived and the previous one finished.  Returns the
+    latencies (ms, arrival to results in host memory), the span (s) and the
+    service time of every query (s)."""
+    import queue
+    import threading
+
+    q = queue.Queue()
+    fin = np.zeros(len(qg))
+    service = np.zeros(len(qg))
+    t0 = time.perf_counter()
+
+    def worker():
+        while True:
+            i = q.get()
+            if i is None:
+                return
+            ts = time.perf_counter()
+            gs[int(qg[i])].bfs(qr[i])
+            fin[i] = time.perf_counter() - t0
+            service[i] = fin[i] - (ts - t0)
+
+    th = threading.Thread(target=worker, daemon=True)
+    th.start()
+    for i, a in enumerate(arrivals):
+        now = time.perf_counter() - t0
+        if a > now:
+            time.sleep(a - now)
+        q.put(i)
+    q.put(None)
+    th.join()
+    return (fin - arrivals) * 1e3, float(fin.max() - arrivals[0]), list(service)
+
+
 def serving_report(args):
     """C5: Poisson arrivals of (graph, root) queries over resident graphs,
     swept rate; the server (continuous batching) against the plain path
@@ -798,30 +843,25 @@ def serving_report(args):
         deg = np.diff(h.col_ptr)
         nz = np.flatnonzero(deg)
         qr.append(int(nz[int(rng.integers(0, nz.size))]) if nz.size else 0)
-    # plain path: measured service time of every query, one at a time
-    svc, edges = [], []
+    # every graph's workspace warmed once; per-query edges from one
+    # traversal each (not timed)
+    for g in gs:
+        g.bfs(0)
+    edges_total = 0.0
     for gi, r in zip(qg, qr):
-        gs[int(gi)].bfs(r)  # warm the graph's workspace
-    for gi, r in zip(qg, qr):
-        t0 = time.perf_counter()
-        res = gs[int(gi)].bfs(r)
-        svc.append(time.perf_counter() - t0)
-        edges.append(res.stats["edges"] / 2)
-    svc = np.array(svc)
-    edges_total = float(np.sum(edges))
+        edges_total += gs[int(gi)].bfs(r).stats["edges"] / 2
+    svc = []
     rates = [float(x) for x in args.serving_rates.split(",") if x]
     sweep = []
     with tb.Server(max_slots=512, mem_budget=48 << 30) as srv:
         for rate in rates:
             gaps = rng.exponential(1.0 / rate, nq)
             arrivals = np.cumsum(gaps)
-            # plain FIFO single server fed the same arrivals
-            fin, lat_p = 0.0, []
-            for a, sv in zip(arrivals, svc):
-                start = max(a, fin)
-                fin = start + sv
-                lat_p.append(fin - a)
-            plain_span = fin - arrivals[0]
+            # plain path, run for real: one host thread serves the queries
+            # one at a time (tbfs_bfs, results to host memory) in arrival
+            # order, fed at the same arrival times
+            lat_p, plain_span, service = plain_fifo(gs, qg, qr, arrivals)
+            svc.extend(service)
             # server: submit at the arrival times, wait for all
             c0, ts0 = srv.counters(), srv.time_split()
             tickets = []
@@ -842,7 +882,6 @@ def serving_report(args):
             split["routed_queries"] = ts1["plain_runs"] - ts0["plain_runs"]
             split["mean_slots_per_launch"] = round((ts1["slot_sum"] - ts0["slot_sum"]) / nl, 2)
             lat_s = np.array(lat_s)
-            lat_p = np.array(lat_p) * 1e3
             sweep.append({
                 "rate_qps": rate, "queries": nq,
                 "server": {"p50_ms": float(np.percentile(lat_s, 50)),
@@ -871,10 +910,11 @@ def serving_report(args):
                         f"{sum(1 for nm, _ in hs if nm.startswith('grid'))} grids (sides 64..{args.serving_max_side}); "
                         "(graph, root) uniform; Poisson arrivals; S + sigma copied to host per query",
             "graph_bytes": hbm, "generation_s": t_gen,
-            "plain_mean_service_ms": float(svc.mean() * 1e3),
+            "plain_mean_service_ms": float(np.mean(svc) * 1e3),
             "sweep": sweep, "results_identical_to_plain": same,
-            "latency": "submit to results in host memory (server); FIFO replay of measured "
-                       "one-at-a-time service times on the same arrivals (plain)"}
+            "latency": "submit to results in host memory, host wall clock; server: continuous "
+                       "batching; plain: one host thread running tbfs_bfs one query at a time in "
+                       "arrival order on the same arrivals"}
 
 
 def mm_text(h) -> bytes:

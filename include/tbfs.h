@@ -80,6 +80,11 @@ typedef struct tbfs_options {
    * previous level's lists; pull is used unless it reads more than
    * pull_ratio times as many list entries as push.  <= 0: default 4. */
   float pull_ratio;
+  /* Engine shape of the single-source traversal (tbfs_autotune sets both):
+   * the most list entries a lane handles per round of a push or pull (1..6;
+   * 0 = 6), and CTAs per SM of the persistent launch (0 = as many as fit). */
+  int32_t max_ept;
+  int32_t ctas_per_sm;
 } tbfs_options;
 
 typedef struct tbfs_stats {
@@ -258,15 +263,24 @@ typedef struct tbfs_degree_stats {
 tbfs_status tbfs_graph_degree_stats(tbfs_graph *g, int32_t kind, tbfs_degree_stats *out,
                                     int64_t *dist, int64_t dist_cap);
 
-/* Autotuner: picks alpha, beta and pull_ratio for g by timing traversals
- * from the k sample roots (device events; each parameter in turn over a
- * short candidate list, starting from opt's values' defaults) and writes
- * them into *opt, leaving its other fields as they are.  With cache_path
- * (a text file; NULL: no cache) the result is stored under a key made of
- * the graph's degree-profile shape, and a later call on a graph with the
- * same key returns the stored values without timing (*from_cache = 1). */
+/* Autotuner: picks the single-source engine's shape (max_ept, ctas_per_sm)
+ * and then alpha, beta and pull_ratio for g by timing traversals from the k
+ * sample roots (device events; the shape over a small grid at opt's
+ * direction parameters, then every combination of a grid of those at the
+ * chosen shape) and writes them into *opt, leaving its other fields as they
+ * are.  With cache_path (a text file; NULL: no cache) the result is stored
+ * under a key made of the graph's degree-profile shape, and a later call on
+ * a graph with the same key returns the stored values without timing
+ * (*from_cache = 1). */
 tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_t k, const char *cache_path,
                           tbfs_options *opt, int32_t *from_cache);
+
+/* The same for tbfs_bfs_batch: picks opt->alpha, the frontier-matrix batch's
+ * push/pull threshold, by timing one batch launch of the k (<= 256) roots per
+ * candidate (with or without path counts as opt->want_sigma); cached per
+ * degree-profile shape and root count. */
+tbfs_status tbfs_autotune_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
+                                const char *cache_path, tbfs_options *opt, int32_t *from_cache);
 
 /* Betweenness centrality over the given roots: bc[v] = sum over roots s != v
  * of Brandes' dependency delta_s(v) (U. Brandes, J. Math. Sociology 25(2),

@@ -59,7 +59,7 @@ def test_version_and_status_strings():
 
 def test_options_layout_and_defaults():
     o = tb.make_options()
-    assert ctypes.sizeof(_lib.Options) == 56 and ctypes.sizeof(_lib.Stats) == 40
+    assert ctypes.sizeof(_lib.Options) == 64 and ctypes.sizeof(_lib.Stats) == 40
     assert o.mode == 0 and o.want_sigma == 1 and o.alpha == 15.0 and o.beta == 18.0
 
 

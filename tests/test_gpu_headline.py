@@ -57,13 +57,14 @@ def _validate_all(g, roots, S, sg, stats):
 
 
 @pytest.mark.parametrize("params", [{}, {"alpha": 9, "beta": 2, "pull_ratio": 2},
-                                    {"alpha": 9, "beta": 1, "pull_ratio": 2}, "autotuned"],
-                         ids=["default", "tuned_b2", "tuned_b1", "autotuned"])
+                                    {"alpha": 9, "beta": 1, "pull_ratio": 2},
+                                    {"max_ept": 2, "ctas_per_sm": 2}, "autotuned"],
+                         ids=["default", "tuned_b2", "tuned_b1", "shape", "autotuned"])
 def test_all_64_roots_validate(headline, params):
     h, roots, g, S, sg = headline
     if params == "autotuned":
         tu = g.autotune(roots[:8])
-        params = {"alpha": tu["alpha"], "beta": tu["beta"], "pull_ratio": tu["pull_ratio"]}
+        params = {k: v for k, v in tu.items() if k != "from_cache"}
     stats = _run_many(g, roots, S, sg, **params)
     assert all(s["bu_levels"] >= 1 for s in stats)
     _validate_all(g, roots, S, sg, stats)

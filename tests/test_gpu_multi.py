@@ -115,13 +115,18 @@ def _queries(hs, count, seed):
 
 
 def test_server_results_equal_alone(gpu_available, served_graphs):
+    """Results of queries that shared launches with others (in the mix) equal
+    the same queries run alone: the launches must actually have carried more
+    than one query each on average."""
     hs, gs = served_graphs
     qs = _queries(hs, 120, seed=1)
     with tb.Server(max_slots=64, mem_budget=1 << 30) as srv:
         tickets = [srv.submit(gs[gi], r) for gi, r in qs]
         results = [srv.wait(t) for t in tickets]
         c = srv.counters()
+        split = srv.time_split()
         assert c["completed"] == len(qs) and c["launches"] >= 1
+        assert split["slot_sum"] / c["launches"] > 1.0, (split, c)
     for (gi, r), (res, lat) in zip(qs, results):
         alone = gs[gi].bfs(r)
         assert np.array_equal(res.S, alone.S), (gi, r)

@@ -38,13 +38,44 @@ def test_autotune_candidates_cache_and_results(gpu_available, tmp_path):
         assert t1["alpha"] in (4.0, 6.0, 9.0, 12.0, 15.0, 24.0, 60.0)
         assert t1["beta"] in (1.0, 2.0, 4.0, 18.0)
         assert t1["pull_ratio"] in (0.5, 1.0, 2.0, 4.0)
+        assert t1["max_ept"] in (2, 4, 0) and t1["ctas_per_sm"] in (1, 2, 0)
         t2 = g.autotune(roots, cache=cache)
-        assert t2["from_cache"] and (t2["alpha"], t2["beta"], t2["pull_ratio"]) == \
-            (t1["alpha"], t1["beta"], t1["pull_ratio"])
+        keys = ("alpha", "beta", "pull_ratio", "max_ept", "ctas_per_sm")
+        assert t2["from_cache"] and all(t2[k] == t1[k] for k in keys)
         # the same family and scale shares the key
         with tb.Graph.from_host_csc(graphs.rmat(15, 16, seed=4)) as g2:
             assert g2.autotune(graphs.pick_roots(h, 1, seed=1), cache=cache)["from_cache"]
         base = g.bfs(int(roots[0]))
-        tuned = g.bfs(int(roots[0]), alpha=t1["alpha"], beta=t1["beta"],
-                      pull_ratio=t1["pull_ratio"])
+        tuned = g.bfs(int(roots[0]), **{k: t1[k] for k in keys})
         assert np.array_equal(base.S, tuned.S) and np.array_equal(base.sigma, tuned.sigma)
+
+
+@pytest.mark.parametrize("max_ept", [1, 2, 4, 0])
+@pytest.mark.parametrize("ctas_per_sm", [1, 2, 0])
+def test_engine_shapes_exact(gpu_available, max_ept, ctas_per_sm):
+    """Every engine shape the autotuner may pick gives the exact result, in
+    every direction mode."""
+    import oracle
+
+    h = graphs.rmat(17, 16, seed=6)
+    with tb.Graph.from_host_csc(h) as g:
+        for r in graphs.pick_roots(h, 2, seed=6):
+            S, sg, ovf, _ = oracle.exact_bfs(h.col_ptr, h.row_idx, int(r))
+            for mode in ("auto", "td", "bu"):
+                res = g.bfs(int(r), mode=mode, max_ept=max_ept, ctas_per_sm=ctas_per_sm)
+                assert np.array_equal(res.S, S)
+                assert np.array_equal(res.sigma[ovf == 0], sg[ovf == 0])
+
+
+def test_autotune_batch(gpu_available, tmp_path):
+    h = graphs.rmat(14, 16, seed=5)
+    roots = graphs.pick_roots(h, 64, seed=5)
+    cache = str(tmp_path / "tune.txt")
+    with tb.Graph.from_host_csc(h) as g:
+        t1 = g.autotune_batch(roots, cache=cache)
+        assert not t1["from_cache"] and t1["alpha"] in (3.0, 5.0, 8.0, 15.0, 30.0)
+        t2 = g.autotune_batch(roots, cache=cache)
+        assert t2["from_cache"] and t2["alpha"] == t1["alpha"]
+        S0, sg0, _ = g.bfs_batch(roots)
+        S1, sg1, _ = g.bfs_batch(roots, alpha=t1["alpha"])
+        assert np.array_equal(S0, S1) and np.array_equal(sg0, sg1)

@@ -46,6 +46,8 @@ class Options(ctypes.Structure):
         ("level_trace", POINTER(c_int64)),
         ("level_trace_cap", c_int32),
         ("pull_ratio", c_float),
+        ("max_ept", c_int32),
+        ("ctas_per_sm", c_int32),
     ]
 
 
@@ -140,6 +142,8 @@ _SIGNATURES = {
     "tbfs_graph_get_cooc": (c_int, [c_void_p, _P_I32, _P_I32]),
     "tbfs_autotune": (c_int, [c_void_p, _P_I32, c_int32, c_char_p, POINTER(Options),
                               POINTER(c_int32)]),
+    "tbfs_autotune_batch": (c_int, [c_void_p, _P_I32, c_int32, c_char_p, POINTER(Options),
+                                    POINTER(c_int32)]),
     "tbfs_brandes": (c_int, [c_void_p, _P_I32, c_int32, POINTER(Options), c_void_p,
                              POINTER(c_int32)]),
     "tbfs_arena_create": (c_int, [c_int32, _P_I32, _P_I64, _P_I32, _P_I32, c_uint32,

@@ -44,7 +44,7 @@ def _flags(symmetric: bool, keep_order: bool) -> int:
 
 def make_options(mode="auto", sigma=True, alpha=None, beta=None, timeout_ns=0,
                  outputs_on_device=False, stream=None, inject_barrier_skip=0,
-                 pull_ratio=None) -> Options:
+                 pull_ratio=None, max_ept=None, ctas_per_sm=None) -> Options:
     o = Options()
     lib().tbfs_options_init(ctypes.byref(o))
     o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
@@ -59,6 +59,10 @@ def make_options(mode="auto", sigma=True, alpha=None, beta=None, timeout_ns=0,
     o.inject_barrier_skip = int(inject_barrier_skip)
     if pull_ratio is not None:
         o.pull_ratio = float(pull_ratio)
+    if max_ept is not None:
+        o.max_ept = int(max_ept)
+    if ctas_per_sm is not None:
+        o.ctas_per_sm = int(ctas_per_sm)
     return o
 
 
@@ -313,7 +317,20 @@ class Graph:
                                   cache.encode() if cache else None, ctypes.byref(o),
                                   ctypes.byref(fc)), "tbfs_autotune")
         return {"alpha": o.alpha, "beta": o.beta, "pull_ratio": o.pull_ratio,
+                "max_ept": o.max_ept, "ctas_per_sm": o.ctas_per_sm,
                 "from_cache": bool(fc.value)}
+
+    def autotune_batch(self, roots, cache: str | None = None, sigma: bool = True, **kw) -> dict:
+        """Tuned {'alpha', 'from_cache'} of the frontier-matrix batch for
+        these (<= 256) roots (timed batch launches; cached per degree profile
+        and root count in ``cache``)."""
+        roots = _i32(roots)
+        o = make_options("auto", sigma, **kw)
+        fc = ctypes.c_int32()
+        check(lib().tbfs_autotune_batch(self.handle, _ptr(roots, _P_I32), int(roots.shape[0]),
+                                        cache.encode() if cache else None, ctypes.byref(o),
+                                        ctypes.byref(fc)), "tbfs_autotune_batch")
+        return {"alpha": o.alpha, "from_cache": bool(fc.value)}
 
     def betweenness(self, roots=None, **kw):
         """Brandes betweenness over ``roots`` (default: every vertex):

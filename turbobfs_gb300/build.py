@@ -115,6 +115,8 @@ def build_oracle(verbose: bool = False) -> Path:
     ref = Path(os.environ.get("TBFS_REFERENCE") or "/root/reference")
     if (ref / "TurboBFS_CSC_TD").is_dir():
         _run(["make", "-C", str(odir), "ref", f"REF={ref}", f"NVCC={nvcc_path()}"], verbose)
+        if LIB.exists():
+            _run(["make", "-C", str(odir), "ref-dropin", f"REF={ref}"], verbose)
     return odir / "liboracle.so"
 
 

@@ -107,8 +107,6 @@ static void graph_free(tbfs_graph *g) {
   }
   tbfs::dev_free(g->cp);
   tbfs::dev_free(g->ic);
-  tbfs::dev_free(g->pull_hubs);
-  tbfs::dev_free(g->pull_hub_seg);
   tbfs::dev_free(g->queues);
   tbfs::dev_free(g->hot); /* bitmaps, S_work, sigma_work */
   tbfs::dev_free(g->inv);
@@ -150,13 +148,11 @@ static tbfs_status graph_finish(tbfs_graph *g) {
   const size_t n = (size_t)g->n;
   CUDA_TRY(tbfs::dev_alloc(&g->queues, 9 * n * sizeof(int)));
   /* the arrays the traversal gathers from at random -- path counts, depths,
-   * frontier bitmaps -- in one block, so that one L2 access-policy window
-   * can cover them (bfs_engine.cu) */
+   * frontier bitmaps -- in one block */
   const size_t sig_b = g->inv ? n * sizeof(unsigned long long) : 0;
   const size_t S_b = g->inv ? (n * sizeof(int) + 255) / 256 * 256 : 0;
   const size_t bm_b = 4 * ((n + 31) / 32) * sizeof(unsigned);
   CUDA_TRY(tbfs::dev_alloc(&g->hot, sig_b + S_b + bm_b));
-  g->hot_bytes = sig_b + S_b + bm_b;
   if (g->inv) {
     g->sigma_work = reinterpret_cast<unsigned long long *>(g->hot);
     g->S_work = reinterpret_cast<int *>(g->hot + sig_b);
@@ -168,10 +164,7 @@ static tbfs_status graph_finish(tbfs_graph *g) {
   CUDA_TRY(cudaEventCreate(&g->ev0));
   CUDA_TRY(cudaEventCreate(&g->ev1));
   CUDA_TRY(tbfs::bfs_geometry(g->device, &g->geom));
-  tbfs::bfs_l2_window(g->device, g->hot, g->hot_bytes, &g->geom);
   g->out_edges_total = g->nnz;
-  CUDA_TRY(tbfs::batch_hubs(g->cp, g->n, TBFS_PULL_SEG, &g->pull_hubs, &g->pull_hub_seg,
-                            &g->n_pull_hubs, &g->pull_hub_segs, 0));
   return TBFS_OK;
 }
 
@@ -654,10 +647,8 @@ static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o,
   p.inject_barrier_skip = o.inject_barrier_skip > 0 ? o.inject_barrier_skip : 0;
   p.trace = nullptr;
   p.trace_cap = 0;
-  p.hubs = g->pull_hubs;
-  p.hub_seg = g->pull_hub_seg;
-  p.nhub = g->n_pull_hubs;
-  p.hub_segs = g->pull_hub_segs;
+  p.max_ept = o.max_ept;
+  p.ctas_per_sm = o.ctas_per_sm;
   return p;
 }
 

@@ -69,12 +69,6 @@
 #ifndef TBFS_MIN_BLOCKS
 #define TBFS_MIN_BLOCKS 3 /* 3 CTAs of 256 per SM: 80 registers, no spills */
 #endif
-#ifndef TBFS_L2_PERSIST
-#define TBFS_L2_PERSIST 0 /* L2 access-policy window over sigma, S and the bitmaps */
-#endif
-#ifndef TBFS_TILE_PULL
-#define TBFS_TILE_PULL 0 /* 1: path counts of bottom-up levels pulled by vertex tiles and hub segments */
-#endif
 
 namespace tbfs {
 namespace {
@@ -348,10 +342,10 @@ struct ExpandPlan {
   unsigned ept, ch, nch;
 };
 
-__device__ __forceinline__ ExpandPlan plan_expand(unsigned qe, unsigned nwarps) {
+__device__ __forceinline__ ExpandPlan plan_expand(unsigned qe, unsigned nwarps, unsigned max_ept) {
   ExpandPlan pl;
   const unsigned per_lane = (qe + 32u * nwarps - 1) / (32u * nwarps);
-  pl.ept = per_lane < 1u ? 1u : (per_lane > (unsigned)kEPT ? (unsigned)kEPT : per_lane);
+  pl.ept = per_lane < 1u ? 1u : (per_lane > max_ept ? max_ept : per_lane);
   const unsigned round = 32u * pl.ept;
   unsigned ch = (qe + 4u * nwarps - 1) / (4u * nwarps);
   ch = (ch + round - 1) / round * round;
@@ -405,149 +399,76 @@ __device__ __forceinline__ void run_expand_item(const BfsParams &p, int d, const
   }
 }
 
-/* Bottom-up phase over tiles of kBuWords consecutive 32-vertex bitmap words;
- * lane i owns vertex 32*word+i of each word, so the depth checks, list
- * bounds and first gathers of all kBuWords vertices are in flight together,
- * and the vertices of one word (consecutive ids, hence similar degrees under
- * the degree grouping, and adjacent lists) advance side by side.
- *   discovery (bu): an unvisited vertex scans its in-list until the first
- *     neighbour in F_d (bitmap cb) -- early exit;
- *   path counts (PULL): a vertex of F_d whose in-list has at most kPullSeg
- *     entries sums sigma over its in-neighbours in F_{d-1} (bitmap pb) --
- *     the whole list, in registers, stored once by the owning lane.
- * Both advance every active vertex of the lane by two list entries per
- * step.  The warp owns its words of the next level's bitmap nb and writes
- * them whole.  Longer lists of F_d are pulled by pull_hub_segment. */
+/* Bottom-up discovery.  A warp takes kBuWords consecutive 32-vertex words
+ * per iteration; lane i owns vertex 32*word+i of each, so the depth checks,
+ * list bounds and the first gathers of all kBuWords vertices are in flight
+ * together.  An unvisited vertex scans its in-list until the first
+ * neighbour in F_d (bitmap cb); the scan advances every still-searching
+ * vertex of the lane by one entry per step.  The warp owns its words of the
+ * next level's bitmap nb and writes them whole. */
 constexpr int kBuWords = 8;
-constexpr int kPullSeg = TBFS_PULL_SEG; /* lists longer than this are pulled in segments */
 
-template <bool PULL>
-__device__ void tile_pass(const BfsParams &p, int d, const NextQueue &nx, const unsigned *cb,
-                          const unsigned *pb, unsigned *nb, unsigned tile, bool bu, bool &ovf) {
+__device__ void bu_tile(const BfsParams &p, int d, const NextQueue &nx, const unsigned *cb,
+                        unsigned *nb, unsigned tile) {
   const int lane = threadIdx.x & 31;
   const unsigned nwords = ((unsigned)p.n + 31u) >> 5;
-  int k[kBuWords], ke[kBuWords];
-  unsigned long long sum[kBuWords];
-  unsigned search = 0; /* bit j: vertex j unvisited and still searching */
-  unsigned pull = 0;   /* bit j: vertex j in F_d, short list, entries left */
-#pragma unroll
-  for (int j = 0; j < kBuWords; ++j) {
-    const int v = (int)((tile * kBuWords + j) * 32u + (unsigned)lane);
-    k[j] = 0;
-    ke[j] = 0;
-    sum[j] = 0ull;
-    const int sv = v < p.n ? p.S[v] : -2;
-    if (bu && sv == -1) search |= 1u << j;
-    if (PULL && sv == d) pull |= 1u << j;
-  }
-#pragma unroll
-  for (int j = 0; j < kBuWords; ++j)
-    if (((search | pull) >> j) & 1u) {
-      const int v = (int)((tile * kBuWords + j) * 32u + (unsigned)lane);
-      k[j] = __ldg(p.cp + v);
-      ke[j] = __ldg(p.cp + v + 1);
-      if (PULL && ke[j] - k[j] > kPullSeg) pull &= ~(1u << j); /* a hub: by segments */
-    }
-  const unsigned pulled = pull;
-  unsigned found = 0;
-  while (search | pull) { /* two list entries per active vertex per step */
-    int u0[kBuWords], u1[kBuWords];
-    unsigned w0[kBuWords], w1[kBuWords];
+  {
+    int v[kBuWords], k[kBuWords], ke[kBuWords];
+    unsigned search = 0; /* bit j: vertex j unvisited and still searching */
 #pragma unroll
     for (int j = 0; j < kBuWords; ++j) {
-      if ((((search | pull) >> j) & 1u) && k[j] >= ke[j]) { /* list exhausted */
-        search &= ~(1u << j);
-        pull &= ~(1u << j);
-      }
-      const bool on = ((search | pull) >> j) & 1u;
-      u0[j] = on ? __ldg(p.ic + k[j]) : 0;
-      u1[j] = (on && k[j] + 1 < ke[j]) ? __ldg(p.ic + k[j] + 1) : -1;
+      v[j] = (int)((tile * kBuWords + j) * 32u + (unsigned)lane);
+      k[j] = 0;
+      ke[j] = 0;
+      if (v[j] < p.n && p.S[v[j]] == -1) search |= 1u << j;
     }
-#pragma unroll
-    for (int j = 0; j < kBuWords; ++j) { /* frontier words: F_d to search, F_{d-1} to pull */
-      const unsigned *bm = ((search >> j) & 1u) ? cb : pb;
-      const bool on = ((search | pull) >> j) & 1u;
-      w0[j] = on ? bm[(unsigned)u0[j] >> 5] : 0u;
-      w1[j] = (on && u1[j] >= 0) ? bm[(unsigned)u1[j] >> 5] : 0u;
-    }
-#pragma unroll
-    for (int j = 0; j < kBuWords; ++j) {
-      const bool h0 = (w0[j] >> ((unsigned)u0[j] & 31u)) & 1u;
-      const bool h1 = u1[j] >= 0 && ((w1[j] >> ((unsigned)u1[j] & 31u)) & 1u);
-      if ((search >> j) & 1u) {
-        if (h0 || h1) {
-          found |= 1u << j;
-          search &= ~(1u << j);
-        } else {
-          k[j] += 2;
-        }
-      } else if (PULL && ((pull >> j) & 1u)) {
-        const unsigned long long c0 = h0 ? p.sigma[u0[j]] : 0ull;
-        const unsigned long long c1 = h1 ? p.sigma[u1[j]] : 0ull;
-        sum[j] = add_chk(add_chk(sum[j], c0, ovf), c1, ovf);
-        k[j] += 2;
-      }
-    }
-  }
-  if (PULL) {
 #pragma unroll
     for (int j = 0; j < kBuWords; ++j)
-      if ((pulled >> j) & 1u) p.sigma[(tile * kBuWords + j) * 32u + (unsigned)lane] = sum[j];
-  }
-  if (!bu) return;
-  int v[kBuWords], dg[kBuWords], ad[kBuWords];
+      if ((search >> j) & 1u) {
+        k[j] = __ldg(p.cp + v[j]);
+        ke[j] = __ldg(p.cp + v[j] + 1);
+      }
+    unsigned found = 0;
+    while (search) { /* two list entries per searching vertex per step */
+      int u0[kBuWords], u1[kBuWords];
 #pragma unroll
-  for (int j = 0; j < kBuWords; ++j) {
-    v[j] = (int)((tile * kBuWords + j) * 32u + (unsigned)lane);
-    dg[j] = 0;
-    ad[j] = 0;
-    if ((found >> j) & 1u) {
-      p.S[v[j]] = d + 1;
-      ad[j] = __ldg(p.rp + v[j]);
-      dg[j] = __ldg(p.rp + v[j] + 1) - ad[j];
+      for (int j = 0; j < kBuWords; ++j) {
+        if (((search >> j) & 1u) && k[j] >= ke[j]) search &= ~(1u << j); /* list exhausted */
+        const bool on = (search >> j) & 1u;
+        u0[j] = on ? __ldg(p.ic + k[j]) : 0;
+        u1[j] = (on && k[j] + 1 < ke[j]) ? __ldg(p.ic + k[j] + 1) : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < kBuWords; ++j) {
+        if ((search >> j) & 1u) {
+          if (bit_of(cb, u0[j]) || (u1[j] >= 0 && bit_of(cb, u1[j]))) {
+            found |= 1u << j;
+            search &= ~(1u << j);
+          } else {
+            k[j] += 2;
+          }
+        }
+      }
     }
+    int dg[kBuWords], ad[kBuWords];
+#pragma unroll
+    for (int j = 0; j < kBuWords; ++j) {
+      dg[j] = 0;
+      ad[j] = 0;
+      if ((found >> j) & 1u) {
+        p.S[v[j]] = d + 1;
+        ad[j] = __ldg(p.rp + v[j]);
+        dg[j] = __ldg(p.rp + v[j] + 1) - ad[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kBuWords; ++j) {
+      const unsigned word = __ballot_sync(FULL, (found >> j) & 1u);
+      const unsigned wi = tile * kBuWords + j;
+      if (lane == 0 && wi < nwords) nb[wi] = word;
+    }
+    warp_append<kBuWords>(found, v, dg, ad, nx.q, nx.e, nx.a, nx.ctr);
   }
-#pragma unroll
-  for (int j = 0; j < kBuWords; ++j) {
-    const unsigned word = __ballot_sync(FULL, (found >> j) & 1u);
-    const unsigned wi = tile * kBuWords + j;
-    if (lane == 0 && wi < nwords) nb[wi] = word;
-  }
-  warp_append<kBuWords>(found, v, dg, ad, nx.q, nx.e, nx.a, nx.ctr);
-}
-
-/* Path counts of a hub of F_d (in-list longer than kPullSeg): one segment
- * of kPullSeg entries per work item.  The lanes stride the segment
- * (coalesced list reads), test each entry against F_{d-1} (bitmap pb),
- * gather the parents' counts, reduce across the warp and add the segment's
- * sum into sigma[hub]. */
-__device__ void pull_hub_segment(const BfsParams &p, int d, const unsigned *pb, unsigned item,
-                                 bool &ovf) {
-  const int lane = threadIdx.x & 31;
-  const unsigned h = warp_find_owner(p.hub_seg, (unsigned)p.nhub, item);
-  const int v = __ldg(p.hubs + h);
-  if (p.S[v] != d) return; /* same value in every lane */
-  const int b = __ldg(p.cp + v) + (int)(item - (unsigned)__ldg(p.hub_seg + h)) * kPullSeg;
-  const int ce = __ldg(p.cp + v + 1);
-  const int e = b + kPullSeg < ce ? b + kPullSeg : ce;
-  constexpr int kPer = kPullSeg / 32;
-  int u[kPer];
-  unsigned w[kPer];
-#pragma unroll
-  for (int j = 0; j < kPer; ++j) {
-    const int t = b + lane + 32 * j;
-    u[j] = t < e ? __ldg(p.ic + t) : -1;
-  }
-#pragma unroll
-  for (int j = 0; j < kPer; ++j) w[j] = u[j] >= 0 ? pb[(unsigned)u[j] >> 5] : 0u;
-  unsigned long long sum = 0;
-#pragma unroll
-  for (int j = 0; j < kPer; ++j)
-    if (u[j] >= 0 && ((w[j] >> ((unsigned)u[j] & 31u)) & 1u))
-      sum = add_chk(sum, p.sigma[u[j]], ovf);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) sum = add_chk(sum, __shfl_xor_sync(FULL, sum, o), ovf);
-  if (lane == 0 && sum) add_chk(atomicAdd(p.sigma + v, sum), sum, ovf);
 }
 
 __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel(const BfsParams p) {
@@ -638,7 +559,6 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     /* work counter of phase d+2 (last used in phase d-2) */
     if (gtid == 0) ctl->work[(d + 2) & 3] = 0u;
     bool next_ready = false;
-    bool tile_pull = false;
 
     /* this phase's work: up to two expansions, then bottom-up tiles */
     ExpandTask A = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}};
@@ -659,20 +579,18 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     } else {
       ++bu;
       if (want_sigma && !sig_ready) { /* sigma(F_d): pull unless push reads far less */
-        if (p.symmetric && (double)qe <= (double)p.pull_ratio * (double)prev_qe) {
-          if (TBFS_TILE_PULL && p.hubs) tile_pull = true; /* with the discovery tiles */
-          else A.kind = EX_PULL;
-        } else {
+        if (p.symmetric && (double)qe <= (double)p.pull_ratio * (double)prev_qe)
+          A.kind = EX_PULL;
+        else
           A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}};
-        }
       }
     }
-    if (A.kind != EX_NONE) A.pl = plan_expand(A.Q.qe, nwarps);
-    if (B.kind != EX_NONE) B.pl = plan_expand(B.Q.qe, nwarps);
+    const unsigned max_ept =
+        p.max_ept > 0 && p.max_ept < kEPT ? (unsigned)p.max_ept : (unsigned)kEPT;
+    if (A.kind != EX_NONE) A.pl = plan_expand(A.Q.qe, nwarps, max_ept);
+    if (B.kind != EX_NONE) B.pl = plan_expand(B.Q.qe, nwarps, max_ept);
     const unsigned n_tiles = dir == DIR_BU ? (nwords + kBuWords - 1) / kBuWords : 0u;
-    const unsigned n_hub = tile_pull ? (unsigned)p.hub_segs : 0u;
-    const unsigned n_a = A.pl.nch, n_ab = n_a + B.pl.nch, n_h = n_ab + n_hub,
-                   n_all = n_h + n_tiles;
+    const unsigned n_a = A.pl.nch, n_ab = n_a + B.pl.nch, n_all = n_ab + n_tiles;
     unsigned *wctr = &ctl->work[d & 3];
     const int lane = threadIdx.x & 31;
     /* work items: the first statically (global warp index), the rest from
@@ -682,9 +600,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     while (item < n_all) {
       if (item < n_a) run_expand_item(p, d, A, item, nx, bm_next, win, ovf);
       else if (item < n_ab) run_expand_item(p, d, B, item - n_a, nx, bm_next, win, ovf);
-      else if (item < n_h) pull_hub_segment(p, d, bm_prev, item - n_ab, ovf);
-      else if (tile_pull) tile_pass<true>(p, d, nx, bm_cur, bm_prev, bm_next, item - n_h, true, ovf);
-      else tile_pass<false>(p, d, nx, bm_cur, bm_prev, bm_next, item - n_h, true, ovf);
+      else bu_tile(p, d, nx, bm_cur, bm_next, item - n_ab);
       if (n_all <= nwarps) break;
       unsigned nxt = 0;
       if (lane == 0) nxt = nwarps + atomicAdd(wctr, 1u);
@@ -744,53 +660,18 @@ cudaError_t bfs_geometry(int device, LaunchGeom *out) {
   if (per < 1) return cudaErrorInvalidConfiguration;
   out->block = kBlock;
   out->grid = sms * per;
+  out->sms = sms;
+  out->per_sm = per;
   return cudaSuccess;
 }
 
-void bfs_l2_window(int device, void *base, size_t bytes, LaunchGeom *g) {
-  g->l2_bytes = 0;
-  if (!TBFS_L2_PERSIST || !base || bytes == 0) return;
-  int max_win = 0, max_persist = 0;
-  if (cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, device) != cudaSuccess ||
-      cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, device) !=
-          cudaSuccess || max_win <= 0 || max_persist <= 0) {
-    cudaGetLastError();
-    return;
-  }
-  /* the context's persisting carve-out: as much as the device allows (a
-   * limit of this process's context; it ends with the context) */
-  size_t cur = 0;
-  if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) == cudaSuccess &&
-      cur < (size_t)max_persist)
-    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)max_persist);
-  cudaGetLastError();
-  const size_t win = bytes < (size_t)max_win ? bytes : (size_t)max_win;
-  g->l2_base = base;
-  g->l2_bytes = win;
-  const double r = (double)max_persist / (double)win;
-  g->l2_hit_ratio = r < 1.0 ? (float)r : 1.0f;
-}
-
 cudaError_t bfs_launch(const BfsParams &p, const LaunchGeom &g, cudaStream_t s) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(g.grid);
-  cfg.blockDim = dim3(g.block);
-  cfg.stream = s;
-  cudaLaunchAttribute at[2];
-  at[0].id = cudaLaunchAttributeCooperative;
-  at[0].val.cooperative = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  if (g.l2_bytes) {
-    at[1].id = cudaLaunchAttributeAccessPolicyWindow;
-    at[1].val.accessPolicyWindow.base_ptr = g.l2_base;
-    at[1].val.accessPolicyWindow.num_bytes = g.l2_bytes;
-    at[1].val.accessPolicyWindow.hitRatio = g.l2_hit_ratio;
-    at[1].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    at[1].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    cfg.numAttrs = 2;
-  }
-  return cudaLaunchKernelEx(&cfg, bfs_persistent_kernel, p);
+  /* fewer CTAs per SM than fit when the caller's options ask for it */
+  const int grid =
+      p.ctas_per_sm > 0 && p.ctas_per_sm < g.per_sm ? g.sms * p.ctas_per_sm : g.grid;
+  void *args[] = {const_cast<BfsParams *>(&p)};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(bfs_persistent_kernel),
+                                     dim3(grid), dim3(g.block), args, 0, s);
 }
 
 }  // namespace tbfs

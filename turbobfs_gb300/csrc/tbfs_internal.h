@@ -91,35 +91,21 @@ struct BfsParams {
   const int *perm;
   int *S_out;
   unsigned long long *sigma_out;
-  /* vertices whose in-lists are longer than the pull segment (internal ids)
-   * and the exclusive prefix of their segment counts (nhub + 1); null: the
-   * path counts of bottom-up levels are pulled through the frontier queue */
-  const int *hubs;
-  const int *hub_seg;
-  int nhub, hub_segs;
+  /* engine shape: most list entries per lane and round (0: the compiled
+   * maximum), CTAs per SM of the launch (0: as many as fit) */
+  int max_ept;
+  int ctas_per_sm;
 };
-
-/* In-list length above which a vertex's path counts are pulled in segments
- * of this many entries by several warps (bfs_engine.cu). */
-#ifndef TBFS_PULL_SEG
-#define TBFS_PULL_SEG 256
-#endif
 
 /* Launch geometry of the persistent kernel on the current device. */
 struct LaunchGeom {
   int grid = 0;
   int block = 0;
-  /* L2 access-policy window of the single-source kernel (0 bytes: none) */
-  void *l2_base = nullptr;
-  size_t l2_bytes = 0;
-  float l2_hit_ratio = 0.0f;
+  int sms = 0, per_sm = 0; /* grid = sms * per_sm */
 };
 
 cudaError_t bfs_launch(const BfsParams &p, const LaunchGeom &g, cudaStream_t s);
 cudaError_t bfs_geometry(int device, LaunchGeom *out);
-/* Mark [base, base + bytes) as persisting in L2 for the single-source
- * kernel's launches (TBFS_L2_PERSIST builds; otherwise leaves g as is). */
-void bfs_l2_window(int device, void *base, size_t bytes, LaunchGeom *g);
 
 /* ---- frontier-matrix batch (batch_engine.cu) ----
  * Up to 256 roots on one graph advance together: bit r of a vertex's row
@@ -314,7 +300,6 @@ struct tbfs_graph {
   /* workspace */
   int *queues = nullptr; /* one allocation: q[3], e[3], a[3], n ints each */
   char *hot = nullptr;   /* one allocation: sigma_work, S_work, bitmaps */
-  size_t hot_bytes = 0;
   unsigned *bitmaps = nullptr; /* four frontier bitmaps, (n+31)/32 words each */
   /* degree-grouped numbering: inv[caller id] = internal id (null: identity);
    * the traversal works on internal S/sigma and un-permutes at the end */
@@ -344,10 +329,6 @@ struct tbfs_graph {
   int many_cap = 0;
   std::vector<cudaEvent_t> many_ev;   /* 2 per root, timing          */
   std::vector<cudaEvent_t> many_sync; /* 2 per root, ready / copied  */
-  /* vertices with in-lists longer than TBFS_PULL_SEG and the exclusive prefix
-   * of their segment counts (see BfsParams) */
-  int *pull_hubs = nullptr, *pull_hub_seg = nullptr;
-  int n_pull_hubs = 0, pull_hub_segs = 0;
   int depth_hint = 0; /* levels of the last traversal of this graph (0: none yet) */
   bool pending = false; /* a traversal was enqueued and not yet collected */
   tbfs_stats last = {};

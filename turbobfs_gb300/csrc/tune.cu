@@ -18,12 +18,14 @@
  * numbering.  The host finishes from the histogram in degree order, so the
  * accumulated distributions are the reference's to the bit.
  *
- * Autotuner: the direction switch (alpha, beta) and the path-count schedule
- * (pull_ratio) of the single-source engine are chosen by timing traversals
- * from sample roots (CUDA events) for every combination of a small grid of
- * candidates (and the defaults).  The winner is cached under a
- * key made of the profile's shape (log2 of n, nnz and the maximum degree,
- * and every histogram bucket rounded to a power of two): graphs of one
+ * Autotuner: the single-source engine's shape (list entries per lane and
+ * round, CTAs per SM), then its direction switch (alpha, beta) and path-count
+ * schedule (pull_ratio) are chosen by timing traversals from sample roots
+ * (CUDA events) over a small grid of candidates; the frontier-matrix batch's
+ * push/pull threshold likewise by timing batch launches.  The winner is
+ * cached under a key made of the profile's shape (log2 of n, nnz and the
+ * maximum degree, and every histogram bucket rounded to a power of two; for
+ * the batch also the root count rounded up to a power of two): graphs of one
  * family and scale share it, so a later call returns without timing.
  */
 #include <cuda_runtime.h>
@@ -142,31 +144,38 @@ std::string profile_key(const tbfs_graph *g, const int64_t *hist, int64_t maxd) 
   return std::string(buf) + (g->separate_out ? "_dir" : "_sym");
 }
 
-bool cache_lookup(const char *path, const std::string &key, float *a, float *b, float *pr) {
+/* a cache line: "key alpha beta pull_ratio [max_ept ctas_per_sm]" */
+struct Tuned {
+  float a = 15.0f, b = 18.0f, pr = 4.0f;
+  int ept = 0, ctas = 0;
+};
+
+bool cache_lookup(const char *path, const std::string &key, Tuned *t) {
   if (!path) return false;
   std::lock_guard<std::mutex> lk(g_cache_mu);
   FILE *f = fopen(path, "r");
   if (!f) return false;
-  char k[512];
-  float x, y, z;
+  char line[1024], k[512];
   bool found = false;
-  while (fscanf(f, "%511s %f %f %f", k, &x, &y, &z) == 4)
-    if (key == k) { /* the last entry for the key wins */
-      *a = x;
-      *b = y;
-      *pr = z;
+  while (fgets(line, sizeof line, f)) {
+    Tuned x;
+    const int got = sscanf(line, "%511s %f %f %f %d %d", k, &x.a, &x.b, &x.pr, &x.ept, &x.ctas);
+    if (got >= 4 && key == k) { /* the last entry for the key wins */
+      if (got < 6) x.ept = x.ctas = 0;
+      *t = x;
       found = true;
     }
+  }
   fclose(f);
   return found;
 }
 
-void cache_store(const char *path, const std::string &key, float a, float b, float pr) {
+void cache_store(const char *path, const std::string &key, const Tuned &t) {
   if (!path) return;
   std::lock_guard<std::mutex> lk(g_cache_mu);
   FILE *f = fopen(path, "a");
   if (!f) return;
-  fprintf(f, "%s %g %g %g\n", key.c_str(), a, b, pr);
+  fprintf(f, "%s %g %g %g %d %d\n", key.c_str(), t.a, t.b, t.pr, t.ept, t.ctas);
   fclose(f);
 }
 
@@ -283,6 +292,14 @@ extern "C" tbfs_status tbfs_graph_degree_stats(tbfs_graph *g, int32_t kind,
   return TBFS_OK;
 }
 
+static void apply(const tbfs::Tuned &t, tbfs_options *o) {
+  o->alpha = t.a;
+  o->beta = t.b;
+  o->pull_ratio = t.pr;
+  o->max_ept = t.ept;
+  o->ctas_per_sm = t.ctas;
+}
+
 extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_t k,
                                      const char *cache_path, tbfs_options *opt,
                                      int32_t *from_cache) {
@@ -299,16 +316,14 @@ extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_
   tbfs_status st = tbfs_graph_degree_profile(g, hist, &maxd, nullptr);
   if (st != TBFS_OK) return st;
   const std::string key = tbfs::profile_key(g, hist, maxd);
-  float a = 15.0f, b = 18.0f, pr = 4.0f;
+  tbfs::Tuned best;
   if (from_cache) *from_cache = 0;
-  if (tbfs::cache_lookup(cache_path, key, &a, &b, &pr)) {
-    opt->alpha = a;
-    opt->beta = b;
-    opt->pull_ratio = pr;
+  if (tbfs::cache_lookup(cache_path, key, &best)) {
+    apply(best, opt);
     if (from_cache) *from_cache = 1;
     return TBFS_OK;
   }
-  /* time one parameter set: device time of k traversals, outputs on the device */
+  /* time one setting: device time of k traversals, outputs on the device */
   int *S = nullptr;
   unsigned long long *sg = nullptr;
   if (tbfs::dev_alloc(&S, (size_t)k * g->n * sizeof(int)) != cudaSuccess ||
@@ -322,48 +337,130 @@ extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_
   base.outputs_on_device = 1;
   base.level_trace = nullptr;
   base.level_trace_cap = 0;
-  auto time_of = [&](float ta, float tb, float tp, double *ms) -> tbfs_status {
+  auto time_of = [&](const tbfs::Tuned &t, double *ms) -> tbfs_status {
     tbfs_options o = base;
-    o.alpha = ta;
-    o.beta = tb;
-    o.pull_ratio = tp;
-    double best = 1e30;
+    apply(t, &o);
+    double b = 1e30;
     for (int rep = 0; rep < 2; ++rep) { /* the better of two runs */
       tbfs_status s2 = tbfs_bfs_many(g, roots, k, &o, S, reinterpret_cast<int64_t *>(sg), sts.data());
       if (s2 != TBFS_OK) return s2;
-      double t = 0.0;
-      for (const auto &x : sts) t += x.device_ms;
-      best = std::min(best, t);
+      double t2 = 0.0;
+      for (const auto &x : sts) t2 += x.device_ms;
+      b = std::min(b, t2);
     }
-    *ms = best;
+    *ms = b;
     return TBFS_OK;
   };
-  /* every combination of a grid around the values that win on RMAT-like and
-   * mesh-like graphs (coordinate search stalled in a local optimum there) */
   double cur = 0.0;
-  st = time_of(a, b, pr, &cur);
+  st = time_of(best, &cur);
+  auto consider = [&](const tbfs::Tuned &t) {
+    double ms = 0.0;
+    if (st != TBFS_OK) return;
+    if ((st = time_of(t, &ms)) == TBFS_OK && ms < cur) {
+      cur = ms;
+      best = t;
+    }
+  };
+  /* stage 1, the engine's shape at the default direction parameters: list
+   * entries per lane and round, CTAs per SM */
+  const int epts[] = {2, 4, 0};
+  const int ctass[] = {1, 2, 0};
+  const tbfs::Tuned s0 = best;
+  for (int e : epts)
+    for (int c : ctass) {
+      tbfs::Tuned t = s0;
+      t.ept = e;
+      t.ctas = c;
+      if (t.ept != s0.ept || t.ctas != s0.ctas) consider(t);
+    }
+  /* stage 2, every combination of a grid of the direction switch and the
+   * path-count schedule at that shape (a coordinate search over wider lists
+   * stalled in a local optimum on RMAT) */
   const float alphas[] = {4.0f, 6.0f, 9.0f, 12.0f, 15.0f, 24.0f, 60.0f};
   const float betas[] = {1.0f, 2.0f, 4.0f, 18.0f};
   const float ratios[] = {0.5f, 1.0f, 2.0f, 4.0f};
-  const float a0 = a, b0 = b, p0 = pr;
+  const tbfs::Tuned s1 = best;
   for (float xa : alphas)
     for (float xb : betas)
       for (float xp : ratios) {
-        double t = 0.0;
-        if (st != TBFS_OK || (xa == a0 && xb == b0 && xp == p0)) continue;
-        if ((st = time_of(xa, xb, xp, &t)) == TBFS_OK && t < cur) {
-          cur = t;
-          a = xa;
-          b = xb;
-          pr = xp;
-        }
+        tbfs::Tuned t = s1;
+        t.a = xa;
+        t.b = xb;
+        t.pr = xp;
+        if (xa != s1.a || xb != s1.b || xp != s1.pr) consider(t);
       }
   tbfs::dev_free(S);
   tbfs::dev_free(sg);
   if (st != TBFS_OK) return st;
-  opt->alpha = a;
-  opt->beta = b;
-  opt->pull_ratio = pr;
-  tbfs::cache_store(cache_path, key, a, b, pr);
+  apply(best, opt);
+  tbfs::cache_store(cache_path, key, best);
+  return TBFS_OK;
+}
+
+extern "C" tbfs_status tbfs_autotune_batch(tbfs_graph *g, const int32_t *roots, int32_t k,
+                                           const char *cache_path, tbfs_options *opt,
+                                           int32_t *from_cache) {
+  if (!g || !opt || k < 1 || k > TBFS_BATCH_MAX_ROOTS || !roots) {
+    tbfs_set_error("tbfs_autotune_batch: need a graph, options and 1..256 roots");
+    return TBFS_ERR_INVALID_ARG;
+  }
+  for (int32_t i = 0; i < k; ++i)
+    if (roots[i] < 0 || roots[i] >= g->n) {
+      tbfs_set_error("tbfs_autotune_batch: root outside [0, n)");
+      return TBFS_ERR_INVALID_ARG;
+    }
+  int64_t hist[tbfs::kBuckets], maxd = 0;
+  tbfs_status st = tbfs_graph_degree_profile(g, hist, &maxd, nullptr);
+  if (st != TBFS_OK) return st;
+  int kb = 1;
+  while (kb < k) kb *= 2;
+  const std::string key = tbfs::profile_key(g, hist, maxd) + "_batch" + std::to_string(kb) +
+                          (opt->want_sigma ? "s" : "d");
+  tbfs::Tuned t;
+  if (from_cache) *from_cache = 0;
+  if (tbfs::cache_lookup(cache_path, key, &t)) {
+    opt->alpha = t.a;
+    if (from_cache) *from_cache = 1;
+    return TBFS_OK;
+  }
+  int *S = nullptr;
+  unsigned long long *sg = nullptr;
+  if (tbfs::dev_alloc(&S, (size_t)k * g->n * sizeof(int)) != cudaSuccess ||
+      (opt->want_sigma &&
+       tbfs::dev_alloc(&sg, (size_t)k * g->n * sizeof(unsigned long long)) != cudaSuccess)) {
+    tbfs::dev_free(S);
+    tbfs_set_error("tbfs_autotune_batch: out of device memory for the sample outputs");
+    return TBFS_ERR_OUT_OF_MEMORY;
+  }
+  std::vector<tbfs_stats> sts((size_t)k);
+  tbfs_options o = *opt;
+  o.outputs_on_device = 1;
+  o.level_trace = nullptr;
+  o.level_trace_cap = 0;
+  /* the push/pull threshold of the frontier-matrix batch; one launch per
+   * setting, the better of two */
+  const float alphas[] = {3.0f, 5.0f, 8.0f, 15.0f, 30.0f};
+  double best_ms = 1e30;
+  float best_a = opt->alpha > 0.0f ? opt->alpha : 15.0f;
+  for (float a : alphas) {
+    o.alpha = a;
+    double ms = 1e30;
+    for (int rep = 0; rep < 2 && st == TBFS_OK; ++rep) {
+      st = tbfs_bfs_batch(g, roots, k, &o, TBFS_LAYOUT_ROOT_MAJOR, S,
+                          reinterpret_cast<int64_t *>(sg), sts.data());
+      if (st == TBFS_OK) ms = std::min(ms, sts[0].device_ms);
+    }
+    if (st != TBFS_OK) break;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_a = a;
+    }
+  }
+  tbfs::dev_free(S);
+  tbfs::dev_free(sg);
+  if (st != TBFS_OK) return st;
+  opt->alpha = best_a;
+  t.a = best_a;
+  tbfs::cache_store(cache_path, key, t);
   return TBFS_OK;
 }
