@@ -277,12 +277,19 @@ def reference_gpu(h, roots, k=4):
     if not oracle.refgpu_available():
         return None
     deg = np.diff(h.col_ptr.astype(np.int64))
-    out = {"kernels": "TurboBFS_CSC_TDBU/bfsgputdbucsc_sc.cu and TurboBFS_CSC_TD/bfsgputdcsc_sc.cu "
-                      "(thread per column), compiled unchanged for sm_103a; the warp-per-column "
-                      "variants are not run (unsynchronised shared-memory staging)",
+    out = {"kernels": "TurboBFS_CSC_TDBU/bfsgputdbucsc_sc.cu, TurboBFS_CSC_TD/bfsgputdcsc_sc.cu "
+                      "(thread per column) and TurboBFS_COOC_TD/bfsgputdcooc_sc.cu (thread per "
+                      "entry), compiled unchanged for sm_103a; the warp-per-column variants are "
+                      "not run (unsynchronised shared-memory staging)",
            "roots": k}
+    J = np.repeat(np.arange(h.n, dtype=np.int32), deg)
+
+    def cooc(cp, ic, r):  # edge-parallel COOC kernels; no S, reached = sigma > 0
+        sg, ms, lv = oracle.refgpu_td_cooc_sc(ic, J, h.n, r)
+        return (np.where(sg > 0, 1, -1), None, ms, lv)
+
     for name, fn in (("tdbu_csc_sc", oracle.refgpu_tdbu_csc_sc),
-                     ("td_csc_sc", oracle.refgpu_td_csc_sc)):
+                     ("td_csc_sc", oracle.refgpu_td_csc_sc), ("td_cooc_sc", cooc)):
         fn(h.col_ptr, h.row_idx, int(roots[0]))  # warm-up (module load, first allocations)
         ms, edges, wall = 0.0, 0, 0.0
         for r in roots[:k]:
@@ -291,7 +298,7 @@ def reference_gpu(h, roots, k=4):
             wall += time.perf_counter() - t0
             S, t = res[0], res[2]
             ms += t
-            reached = S >= 0 if name == "tdbu_csc_sc" else (S > 0) | (np.arange(h.n) == r)
+            reached = S >= 0 if name != "td_csc_sc" else (S > 0) | (np.arange(h.n) == r)
             edges += int(deg[reached].sum()) // 2
         out[name] = {"gteps_kernels": edges / (ms * 1e-3) / 1e9, "ms_per_bfs_kernels": ms / k,
                      "ms_per_call_wall": 1e3 * wall / k}
@@ -563,6 +570,7 @@ def run_e2e(h, roots_c, steps, o_dev, edges_per_step, world):
                "path": "tbfs_graph_create_csc (pinned host CSC) + tbfs_bfs_many (pinned host "
                        "S/sigma) + tbfs_graph_destroy per step, host wall clock"}
         out["dropin_pageable"] = dropin_e2e(h, roots_c[:8])
+        out["dropin_cooc_pageable"] = dropin_cooc_e2e(h, roots_c[:2])
         return out
     finally:
         for b in bufs:
@@ -593,6 +601,31 @@ def dropin_e2e(h, roots):
             "ms_per_call": 1e3 * t / len(roots),
             "h2d_bytes_per_call": 4 * (n + 1) + 4 * nnz, "d2h_bytes_per_call": 8 * n,
             "path": "bfs_gpu_tdbu_csc_sc with pageable numpy arrays, one call per root"}
+
+
+def dropin_cooc_e2e(h, roots):
+    """bfs_gpu_td_cooc_sc (TurboBFS_COOC_TD/bfstdcooc.h:48-49) on the same
+    graph as COOC pairs with pageable host arrays, one call per root: the
+    upload, the sort of the pairs into CSC on the device, the traversal and the
+    float sigma's copy back, host wall clock."""
+    import turbobfs_gb300 as tb
+
+    n, nnz = h.n, h.nnz
+    J = np.repeat(np.arange(n, dtype=np.int32), np.diff(h.col_ptr))
+    sg = np.zeros(n, np.float32)
+    assert tb.bfs_gpu_td_cooc_sc(h.row_idx, J, sg, int(roots[0]), nnz, n, 1) == 0
+    deg = np.diff(h.col_ptr.astype(np.int64))
+    t, edges = 0.0, 0
+    for r in roots:
+        t0 = time.perf_counter()
+        assert tb.bfs_gpu_td_cooc_sc(h.row_idx, J, sg, int(r), nnz, n, 1) == 0
+        t += time.perf_counter() - t0
+        reached = (sg > 0) | (np.arange(n) == r)
+        edges += int(deg[reached].sum()) // 2
+    return {"value": edges / t / 1e9, "unit": UNIT, "roots": len(roots),
+            "ms_per_call": 1e3 * t / len(roots),
+            "path": "bfs_gpu_td_cooc_sc with pageable numpy arrays (row, column pairs), one call "
+                    "per root; includes the device sort of the pairs into CSC"}
 
 
 # ------------------------------------------------------------ batched ----

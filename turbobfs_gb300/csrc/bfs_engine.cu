@@ -69,6 +69,9 @@
 #ifndef TBFS_MIN_BLOCKS
 #define TBFS_MIN_BLOCKS 3 /* 3 CTAs of 256 per SM: 80 registers, no spills */
 #endif
+#ifndef TBFS_SPEC_SIGMA
+#define TBFS_SPEC_SIGMA 0 /* pulls load every neighbour's count with its frontier test */
+#endif
 
 namespace tbfs {
 namespace {
@@ -243,6 +246,14 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
 #pragma unroll
       for (int j = 0; j < kEPT; ++j) /* list reads, all in flight */
         if ((valid >> j) & 1u) u[j] = __ldg(p.jr + u[j]);
+      /* pulls: the neighbours' counts loaded beside their frontier tests,
+       * so that a parent's count is not a third dependent round trip; the
+       * counts of non-parents are dropped */
+      unsigned long long cs[kEPT];
+      if (SIG == SIG_PULL && TBFS_SPEC_SIGMA) {
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) cs[j] = ((valid >> j) & 1u) ? p.sigma[u[j]] : 0ull;
+      }
       int su[kEPT];   /* DISC: depth of the neighbour                        */
       unsigned in = 0; /* bit j: neighbour j is in the level the sigma mode needs */
       if (DISC) {
@@ -305,7 +316,8 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
       if (SIG == SIG_PULL) {
         unsigned long long c[kEPT]; /* path counts of the parents only */
 #pragma unroll
-        for (int j = 0; j < kEPT; ++j) c[j] = ((in >> j) & 1u) ? p.sigma[u[j]] : 0ull;
+        for (int j = 0; j < kEPT; ++j)
+          c[j] = ((in >> j) & 1u) ? (TBFS_SPEC_SIGMA ? cs[j] : p.sigma[u[j]]) : 0ull;
         unsigned long long run = 0;
         int rk = kk[0];
 #pragma unroll
