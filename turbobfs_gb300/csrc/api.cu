@@ -165,6 +165,14 @@ static tbfs_status graph_finish(tbfs_graph *g) {
   CUDA_TRY(cudaEventCreate(&g->ev1));
   CUDA_TRY(tbfs::bfs_geometry(g->device, &g->geom));
   g->out_edges_total = g->nnz;
+  {
+    int64_t hist[40], maxd = 0;
+    tbfs_status st = tbfs_graph_degree_profile(g, hist, &maxd, nullptr);
+    if (st != TBFS_OK) return st;
+    int b = 0;
+    while (b < 63 && (1ll << b) <= maxd) ++b; /* maxd < 2^b */
+    g->deg_bits = b;
+  }
   return TBFS_OK;
 }
 
@@ -649,6 +657,7 @@ static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o,
   p.trace_cap = 0;
   p.max_ept = o.max_ept;
   p.ctas_per_sm = o.ctas_per_sm;
+  p.deg_bits = g->deg_bits;
   return p;
 }
 

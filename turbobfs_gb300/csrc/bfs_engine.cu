@@ -69,8 +69,8 @@
 #ifndef TBFS_MIN_BLOCKS
 #define TBFS_MIN_BLOCKS 3 /* 3 CTAs of 256 per SM: 80 registers, no spills */
 #endif
-#ifndef TBFS_SPEC_SIGMA
-#define TBFS_SPEC_SIGMA 0 /* pulls load every neighbour's count with its frontier test */
+#ifndef TBFS_RED_PUSH
+#define TBFS_RED_PUSH 1 /* pushes without the overflow check where a bound rules overflow out */
 #endif
 
 namespace tbfs {
@@ -178,7 +178,7 @@ __device__ __forceinline__ bool bit_of(const unsigned *bm, int v) {
  * targets).  Without DISC, membership of a neighbour in the level the mode
  * needs (d-1 for PULL, tgt for PUSH_AT) is read from bitmap tb, one bit per
  * vertex, instead of from S. */
-template <bool DISC, int SIG>
+template <bool DISC, int SIG, bool CHK = true>
 __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt, const Queue &Q,
                                              unsigned E0, unsigned E1, unsigned ept,
                                              const NextQueue &nx, const unsigned *tb,
@@ -246,14 +246,6 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
 #pragma unroll
       for (int j = 0; j < kEPT; ++j) /* list reads, all in flight */
         if ((valid >> j) & 1u) u[j] = __ldg(p.jr + u[j]);
-      /* pulls: the neighbours' counts loaded beside their frontier tests,
-       * so that a parent's count is not a third dependent round trip; the
-       * counts of non-parents are dropped */
-      unsigned long long cs[kEPT];
-      if (SIG == SIG_PULL && TBFS_SPEC_SIGMA) {
-#pragma unroll
-        for (int j = 0; j < kEPT; ++j) cs[j] = ((valid >> j) & 1u) ? p.sigma[u[j]] : 0ull;
-      }
       int su[kEPT];   /* DISC: depth of the neighbour                        */
       unsigned in = 0; /* bit j: neighbour j is in the level the sigma mode needs */
       if (DISC) {
@@ -309,15 +301,15 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
           if (add) {
             const unsigned long long x =
                 ((unsigned long long)w.hi[kk[j]] << 32) | (unsigned long long)w.lo[kk[j]];
-            add_chk(atomicAdd(p.sigma + u[j], x), x, ovf);
+            if (CHK) add_chk(atomicAdd(p.sigma + u[j], x), x, ovf);
+            else atomicAdd(p.sigma + u[j], x); /* result unused: a reduction, no round trip */
           }
         }
       }
       if (SIG == SIG_PULL) {
         unsigned long long c[kEPT]; /* path counts of the parents only */
 #pragma unroll
-        for (int j = 0; j < kEPT; ++j)
-          c[j] = ((in >> j) & 1u) ? (TBFS_SPEC_SIGMA ? cs[j] : p.sigma[u[j]]) : 0ull;
+        for (int j = 0; j < kEPT; ++j) c[j] = ((in >> j) & 1u) ? p.sigma[u[j]] : 0ull;
         unsigned long long run = 0;
         int rk = kk[0];
 #pragma unroll
@@ -383,6 +375,7 @@ struct ExpandTask {
   Queue Q;
   const unsigned *tb;
   ExpandPlan pl;
+  bool chk; /* pushes check every add for overflow */
 };
 
 __device__ __forceinline__ void run_expand_item(const BfsParams &p, int d, const ExpandTask &t,
@@ -395,13 +388,21 @@ __device__ __forceinline__ void run_expand_item(const BfsParams &p, int d, const
       expand_chunk<true, SIG_NONE>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
       break;
     case EX_DISC_PUSH_NEW:
-      expand_chunk<true, SIG_PUSH_NEW>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      if (t.chk)
+        expand_chunk<true, SIG_PUSH_NEW>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      else
+        expand_chunk<true, SIG_PUSH_NEW, false>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb,
+                                                w, ovf);
       break;
     case EX_DISC_PULL:
       expand_chunk<true, SIG_PULL>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
       break;
     case EX_PUSH_AT:
-      expand_chunk<false, SIG_PUSH_AT>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      if (t.chk)
+        expand_chunk<false, SIG_PUSH_AT>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
+      else
+        expand_chunk<false, SIG_PUSH_AT, false>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb,
+                                                w, ovf);
       break;
     case EX_PULL:
       expand_chunk<false, SIG_PULL>(p, d, t.tgt, t.Q, E0, E1, t.pl.ept, nx, t.tb, nb, w, ovf);
@@ -521,6 +522,13 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
   unsigned prev_qn = 0, prev_qe = 0;
   bool ovf = false, sig_ready = true; /* sigma(F_d) final at the start of phase d */
   bool done = false;
+  /* Bound on the bits of the path counts of F_d: sigma(F_0) = 1, and a count
+   * of F_{d+1} sums at most max-in-degree counts of F_d, so it has at most
+   * deg_bits more bits.  Pushes into a level whose bound is at most 63 bits
+   * cannot overflow and add without the check (a reduction whose result
+   * is not waited for); so do pushes once an overflow has been recorded,
+   * since the flag is per traversal. */
+  int sig_bits = 1;
   for (;;) {
     const unsigned long long cur = __ldcg(&ctl->qctr[d % 3]);
     const unsigned qn = (unsigned)(cur >> 32);
@@ -573,8 +581,8 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     bool next_ready = false;
 
     /* this phase's work: up to two expansions, then bottom-up tiles */
-    ExpandTask A = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}};
-    ExpandTask B = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}};
+    ExpandTask A = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}, true};
+    ExpandTask B = {EX_NONE, 0, Qc, bm_prev, {1, 1, 0}, true};
     if (dir == DIR_TD) {
       ++td;
       if (!want_sigma) {
@@ -585,7 +593,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
       } else if (p.symmetric) { /* finish sigma(F_d) on the same list reads */
         A.kind = EX_DISC_PULL;
       } else { /* sigma(F_d) from F_{d-1}'s out-lists, discovery from F_d */
-        A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}};
+        A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}, true};
         B.kind = EX_DISC;
       }
     } else {
@@ -594,11 +602,18 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
         if (p.symmetric && (double)qe <= (double)p.pull_ratio * (double)prev_qe)
           A.kind = EX_PULL;
         else
-          A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}};
+          A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}, true};
       }
     }
     const unsigned max_ept =
         p.max_ept > 0 && p.max_ept < kEPT ? (unsigned)p.max_ept : (unsigned)kEPT;
+    if (TBFS_RED_PUSH && want_sigma) {
+      const bool ovf_seen = dev::ld_volatile(&ctl->sigma_overflow) != 0;
+      const int nb_next = sig_bits + p.deg_bits; /* bound of F_{d+1} */
+      if (A.kind == EX_DISC_PUSH_NEW)
+        A.chk = !ovf_seen && !(p.deg_bits > 0 && nb_next <= 63);
+      if (A.kind == EX_PUSH_AT) A.chk = !ovf_seen && !(p.deg_bits > 0 && sig_bits <= 63);
+    }
     if (A.kind != EX_NONE) A.pl = plan_expand(A.Q.qe, nwarps, max_ept);
     if (B.kind != EX_NONE) B.pl = plan_expand(B.Q.qe, nwarps, max_ept);
     const unsigned n_tiles = dir == DIR_BU ? (nwords + kBuWords - 1) / kBuWords : 0u;
@@ -622,8 +637,13 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     prev_qe = qe;
     /* test hook: CTA 0 leaves without arriving; the others' waits expire */
     if (p.inject_barrier_skip > 0 && blockIdx.x == 0 && d == p.inject_barrier_skip - 1) return;
+    if (TBFS_RED_PUSH && want_sigma) { /* overflow recorded now: seen by every CTA after the barrier */
+      const bool any_ovf = __any_sync(FULL, ovf);
+      if (any_ovf && (threadIdx.x & 31) == 0) atomicOr(&ctl->sigma_overflow, 1);
+    }
     if (!grid_barrier(ctl, p.timeout_ns, d)) break;
     sig_ready = next_ready;
+    sig_bits = sig_bits + p.deg_bits < 64 ? sig_bits + p.deg_bits : 64;
     ++d;
   }
   if (__any_sync(FULL, ovf) && (threadIdx.x & 31) == 0) atomicOr(&ctl->sigma_overflow, 1);

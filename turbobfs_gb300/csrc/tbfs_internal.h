@@ -95,6 +95,9 @@ struct BfsParams {
    * maximum), CTAs per SM of the launch (0: as many as fit) */
   int max_ept;
   int ctas_per_sm;
+  /* bits of the largest in-degree (0: unknown); bounds the path counts'
+   * growth per level (bfs_engine.cu) */
+  int deg_bits;
 };
 
 /* Launch geometry of the persistent kernel on the current device. */
@@ -300,6 +303,7 @@ struct tbfs_graph {
   /* workspace */
   int *queues = nullptr; /* one allocation: q[3], e[3], a[3], n ints each */
   char *hot = nullptr;   /* one allocation: sigma_work, S_work, bitmaps */
+  int deg_bits = 0;      /* bits of the largest in-degree */
   unsigned *bitmaps = nullptr; /* four frontier bitmaps, (n+31)/32 words each */
   /* degree-grouped numbering: inv[caller id] = internal id (null: identity);
    * the traversal works on internal S/sigma and un-permutes at the end */
