@@ -102,7 +102,12 @@ void tbfs_options_init(tbfs_options *opt);
 
 /* Upload a CSC adjacency (col_ptr[n+1], row_idx[nnz], int32, 0-based).
  * The graph stays resident until tbfs_graph_destroy.  Without
- * TBFS_GRAPH_SYMMETRIC the transpose (out-lists) is built on the device. */
+ * TBFS_GRAPH_SYMMETRIC the device first tests whether the lists equal their
+ * transpose (the sums over the entries u -> v of h(u, v) - h(v, u) vanish
+ * for two 64-bit hashes with fresh random keys; a graph that is not its own
+ * transpose passes with probability about 2^-128): if so the in-lists serve
+ * as out-lists and tbfs_graph_info reports TBFS_GRAPH_SYMMETRIC, otherwise
+ * the transpose (out-lists) is built on the device. */
 tbfs_status tbfs_graph_create_csc(const int32_t *col_ptr, const int32_t *row_idx,
                                   int32_t n, int64_t nnz, uint32_t flags,
                                   tbfs_graph **out);
@@ -234,7 +239,8 @@ tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40, int64_t *m
  *   TBFS_DEGREE_IN          in-degree (column lengths)
  *   TBFS_DEGREE_OUT         out-degree (row counts)
  *   TBFS_DEGREE_UNDIRECTED  degree_ug's out + in of the graph's entries: the
- *                           column length of a TBFS_GRAPH_SYMMETRIC graph,
+ *                           column length of a graph created with
+ *                           TBFS_GRAPH_SYMMETRIC (or built symmetrised),
  *                           in + out otherwise
  * max_degree / argmax: degree_max (the first vertex, caller numbering, of
  * maximum degree; -1 when every degree is 0).  mean / sd: degree_sta (sum in

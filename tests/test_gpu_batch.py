@@ -148,6 +148,23 @@ def test_batch_overflow_flags_per_root(gpu_available):
             assert flags[0] == 1 and flags[4] == 1
 
 
+@pytest.mark.parametrize("width,layers", [(16, 9), (16, 10), (16, 12), (300, 4), (300, 6)])
+def test_batch_counts_past_32_bits(gpu_available, width, layers):
+    """Launches first keep path counts in 32 bits and are redone with 64-bit
+    counts when one needs more.  Layered graphs (counts up to
+    width^(layers-1)): 16-wide with 2^32, 2^36 and 2^44 paths (redone);
+    300-wide (in-lists of 300-600 entries, split into segments at 20 roots)
+    with 2.7e7 paths (kept in 32 bits) and 2.4e12 (redone).  Exact counts,
+    no overflow flag, in every mode."""
+    h = graphs.layered_bipartite(width, layers)
+    roots = np.arange(0, min(h.n, 20 * 7), 7, dtype=np.int32)[:20]
+    with tb.Graph.from_host_csc(h) as g:
+        for mode in MODES:
+            S, sg, st = g.bfs_batch(roots, mode=mode)
+            _check_roots(h.col_ptr, h.row_idx, roots, S, sg, st)
+            assert not any(x["sigma_overflow"] for x in st)
+
+
 def test_batch_device_outputs(gpu_available):
     torch = pytest.importorskip("torch")
     import ctypes

@@ -5,6 +5,8 @@ must equal the exact oracle on every vertex, in every traversal mode; the
 drop-in entry points must equal the outputs the reference's GPU drivers
 produce (emulated by the oracle, and frozen from the reference's own
 sequential code in tests/golden/ where both are exact)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -288,3 +290,29 @@ def test_barrier_timeout_is_reported_and_context_survives(gpu_available):
         assert e.value.status == 4
         res = g.bfs(0)
         _exact_check(h.col_ptr, h.row_idx, 0, res)
+
+
+# ------------------------------------------------ symmetry found on upload
+
+def test_symmetry_detected_without_the_flag(gpu_available):
+    """A CSC uploaded without TBFS_GRAPH_SYMMETRIC that equals its transpose
+    is found so on the device (tbfs_graph_info then reports the flag) and
+    needs no transpose; one missing mirror entry, or one duplicated on one
+    side only, makes it general.  Results equal the exact oracle either way."""
+    h = graphs.rmat(12, 16, seed=9)
+    col = np.repeat(np.arange(h.n), np.diff(h.col_ptr))
+    variants = {"symmetric": (h.row_idx, col)}
+    keep = np.ones(h.nnz, bool)
+    keep[h.nnz // 3] = False
+    variants["one mirror missing"] = (h.row_idx[keep], col[keep])
+    k = h.nnz // 2
+    variants["one-sided duplicate"] = (np.append(h.row_idx, h.row_idx[k]), np.append(col, col[k]))
+    for name, (src, dst) in variants.items():
+        g2 = graphs.from_edges(h.n, src.astype(np.int32), dst.astype(np.int32))
+        with tb.Graph(g2.col_ptr, g2.row_idx, g2.n, symmetric=False) as g:
+            flags = ctypes.c_uint32()
+            tb.lib().tbfs_graph_info(g.handle, None, None, ctypes.byref(flags))
+            assert bool(flags.value & 1) == (name == "symmetric"), name
+            r = int(graphs.pick_roots(h, 1, seed=9)[0])
+            for mode in MODES:
+                _exact_check(g2.col_ptr, g2.row_idx, r, g.bfs(r, mode=mode))

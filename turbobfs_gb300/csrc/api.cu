@@ -9,6 +9,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
+#include <chrono>
+#include <random>
 #include <vector>
 
 #include "tbfs.h"
@@ -231,9 +234,25 @@ static tbfs_status finish_lists(tbfs_graph *g, int *d_flag) {
       g->perm = perm;
     }
   }
-  if (g->flags & TBFS_GRAPH_SYMMETRIC) {
+  bool symmetric = (g->flags & TBFS_GRAPH_SYMMETRIC) != 0;
+  g->declared_symmetric = symmetric;
+  if (!symmetric && nnz > 0) {
+    /* no promise from the caller: a CSC that equals its transpose needs no
+     * out-lists of its own (fresh random keys each time) */
+    static std::atomic<unsigned long long> calls{0};
+    const unsigned long long salt =
+        (unsigned long long)std::chrono::steady_clock::now().time_since_epoch().count() ^
+        (0x9e3779b97f4a7c15ull * ++calls) ^ (unsigned long long)(uintptr_t)g;
+    std::random_device rd;
+    const unsigned long long k1 = ((unsigned long long)rd() << 32 | rd()) ^ salt;
+    const unsigned long long k2 = ((unsigned long long)rd() << 32 | rd()) ^ (salt * 31);
+    cudaError_t e = tbfs::symmetric_check(g->cp, g->ic, g->n, g->nnz, k1, k2, &symmetric, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "symmetry check", __LINE__);
+  }
+  if (symmetric) {
     g->rp = g->cp;
     g->jr = g->ic;
+    g->flags |= TBFS_GRAPH_SYMMETRIC; /* reported by tbfs_graph_info */
     return TBFS_OK;
   }
   /* out-lists = transpose: key = row id, value = column id */
@@ -889,93 +908,168 @@ extern "C" tbfs_status tbfs_bfs_many(tbfs_graph *g, const int32_t *roots, int32_
 
 namespace {
 
-struct CompatRun {
-  std::vector<int32_t> S;
-  std::vector<int64_t> sigma;
-  tbfs_stats st = {};
-  double total_ms = 0.0;
-  int reps = 0;
-};
+/* What each drop-in entry point hands back (see the table in the header of
+ * tbfs_compat.h): the shim converts the engine's exact int32 depths and
+ * int64 counts on the device and copies the result straight into the
+ * caller's arrays. */
+enum CompatKind { K_TD = 0, K_BU = 1, K_TDBU = 2, K_COOC = 3 };
 
-/* Upload (CSC or COOC), run `repetition` traversals, keep the last result.
- * The graph is treated as general (directed): the caller's arrays carry no
- * symmetry promise. */
+/* TD: S with 0 for unreached (the reference zero-initialises S), float
+ * sigma = the exact count rounded once */
+__global__ void compat_td_kernel(int *S, const unsigned long long *sg, float *out, int n) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    if (S && S[v] < 0) S[v] = 0;
+    out[v] = __ll2float_rn((long long)sg[v]);
+  }
+}
+
+/* vertices per depth d < cap (shared-memory counters, one global add each) */
+__global__ void level_hist_kernel(const int *S, int n, int cap, unsigned long long *cnt) {
+  extern __shared__ unsigned h[];
+  for (int i = threadIdx.x; i < cap; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int d = S[v];
+    if (d >= 0 && d < cap) atomicAdd(&h[d], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < cap; i += blockDim.x)
+    if (h[i]) atomicAdd(cnt + i, (unsigned long long)h[i]);
+}
+
+/* TDBU: int32 sigma (two's-complement wrap of the count) for the depths the
+ * reference expands top-down, 0 beyond */
+__global__ void compat_tdbu_kernel(const int *S, const unsigned long long *sg, int *out, int n,
+                                   int last_td) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int d = S[v];
+    out[v] = (d >= 0 && d <= last_td) ? (int)(unsigned)sg[v] : 0;
+  }
+}
+
+int compat_grid(int n) {
+  const long long b = ((long long)n + 255) / 256;
+  return (int)(b < 2432 ? (b > 0 ? b : 1) : 2432);
+}
+
+/* Upload (CSC or COOC), run `repetition` traversals on the device (the last
+ * one's result is kept, as the reference's drivers keep it), convert and
+ * copy into the caller's S_h / sigma_h.  The graph is uploaded as general:
+ * the caller's arrays carry no symmetry promise (a symmetric one is
+ * recognised on the device and needs no transpose). */
 int compat_run(const int *a, const int *b, bool cooc, int r, int nz, int n, int repetition,
-               bool want_sigma, CompatRun &out) {
+               CompatKind kind, int *S_h, void *sig_h) {
   if (n < 1 || nz < 0 || r < 0 || r >= n || (nz > 0 && (!a || !b)) || (!cooc && !b)) {
     tbfs_set_error("invalid arguments: n=%d nz=%d r=%d", n, nz, r);
     return TBFS_ERR_INVALID_ARG;
   }
+  const bool want_sigma = kind != K_BU;
   tbfs_graph *g = nullptr;
   tbfs_status st = cooc ? tbfs_graph_create_cooc(a, b, n, nz, 0u, &g)
                         : tbfs_graph_create_csc(b, a, n, nz, 0u, &g);
   if (st != TBFS_OK) return st;
+  int *S = nullptr, *out32 = nullptr;
+  unsigned long long *sg = nullptr, *cnt = nullptr;
+  cudaError_t e = tbfs::dev_alloc(&S, (size_t)n * sizeof(int));
+  if (e == cudaSuccess && want_sigma) e = tbfs::dev_alloc(&sg, (size_t)n * sizeof(unsigned long long));
+  if (e == cudaSuccess && want_sigma) e = tbfs::dev_alloc(&out32, (size_t)n * sizeof(int));
   tbfs_options o;
   tbfs_options_init(&o);
   o.want_sigma = want_sigma ? 1 : 0;
-  out.S.assign((size_t)n, 0);
-  if (want_sigma) out.sigma.assign((size_t)n, 0);
-  out.reps = repetition < 1 ? 1 : repetition;
-  for (int i = 0; i < out.reps && st == TBFS_OK; ++i) {
-    st = tbfs_bfs(g, r, &o, out.S.data(), want_sigma ? out.sigma.data() : nullptr, &out.st);
-    out.total_ms += out.st.device_ms;
+  o.outputs_on_device = 1;
+  tbfs_stats sts = {};
+  double total_ms = 0.0;
+  const int reps = repetition < 1 ? 1 : repetition;
+  if (e != cudaSuccess) st = cuda_fail(e, "drop-in buffers", __LINE__);
+  for (int i = 0; i < reps && st == TBFS_OK; ++i) {
+    st = tbfs_bfs(g, r, &o, S, reinterpret_cast<int64_t *>(sg), nullptr);
+    if (st == TBFS_OK) st = tbfs_graph_last_stats(g, &sts);
+    total_ms += sts.device_ms;
   }
+  const int grid = compat_grid(n);
+  if (st == TBFS_OK && kind == K_TD) {
+    compat_td_kernel<<<grid, 256>>>(S, sg, reinterpret_cast<float *>(out32), n);
+    e = cudaGetLastError();
+  } else if (st == TBFS_OK && kind == K_COOC) {
+    compat_td_kernel<<<grid, 256>>>(nullptr, sg, reinterpret_cast<float *>(out32), n);
+    e = cudaGetLastError();
+  } else if (st == TBFS_OK && kind == K_TDBU) {
+    /* The reference's TDBU drivers keep sigma only for the levels they
+     * expand top-down: they stay top-down while the last level held at most
+     * 0.001f*n vertices (a float compare, bfsgputdbucsc_sc.cu:112-122) and
+     * never switch back, and their bottom-up kernel leaves sigma at 0. */
+    const int levels = sts.levels;
+    std::vector<unsigned long long> hc((size_t)levels + 1, 0ull);
+    const int cap = levels + 1 < 8192 ? levels + 1 : 8192;
+    e = tbfs::dev_alloc(&cnt, ((size_t)levels + 1) * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(cnt, 0, ((size_t)levels + 1) * sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+      level_hist_kernel<<<grid, 256, (size_t)cap * sizeof(unsigned)>>>(S, n, cap, cnt);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpy(hc.data(), cnt, ((size_t)levels + 1) * sizeof(unsigned long long),
+                     cudaMemcpyDeviceToHost);
+    const float thr_td = 0.001f;
+    const float thresh_td = thr_td * (float)n;
+    int last_td = levels; /* deepest level reached top-down */
+    for (int d = 1; d < levels && d < cap; ++d)
+      if ((float)hc[(size_t)d] > thresh_td) {
+        last_td = d;
+        break;
+      }
+    if (levels >= cap && last_td == levels) {
+      /* more levels than device counters, none of the first ones past the
+       * threshold: count the deeper levels on the host (graphs over 8192
+       * levels deep only) */
+      std::vector<int> Sh((size_t)n);
+      if (e == cudaSuccess) e = cudaMemcpy(Sh.data(), S, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost);
+      std::vector<long long> c2((size_t)levels + 1, 0);
+      for (int v = 0; v < n; ++v)
+        if (Sh[(size_t)v] >= 0 && Sh[(size_t)v] <= levels) c2[(size_t)Sh[(size_t)v]]++;
+      for (int d = cap; d < levels; ++d)
+        if ((float)c2[(size_t)d] > thresh_td) {
+          last_td = d;
+          break;
+        }
+    }
+    if (e == cudaSuccess) {
+      compat_tdbu_kernel<<<grid, 256>>>(S, sg, out32, n, last_td);
+      e = cudaGetLastError();
+    }
+  }
+  if (st == TBFS_OK && e == cudaSuccess && S_h)
+    e = cudaMemcpy(S_h, S, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost);
+  if (st == TBFS_OK && e == cudaSuccess && want_sigma)
+    e = cudaMemcpy(sig_h, out32, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost);
+  if (st == TBFS_OK && e != cudaSuccess) st = cuda_fail(e, "drop-in results", __LINE__);
+  tbfs::dev_free(cnt);
+  tbfs::dev_free(out32);
+  tbfs::dev_free(sg);
+  tbfs::dev_free(S);
   tbfs_graph_destroy(g);
   if (st == TBFS_OK && getenv("TBFS_PRINT_TIMES"))
-    printf("tbfs: levels = %d, r = %d, average time BFS = %lfms\n", out.st.levels, r,
-           out.total_ms / out.reps);
+    printf("tbfs: levels = %d, r = %d, average time BFS = %lfms\n", sts.levels, r,
+           total_ms / reps);
   return st;
-}
-
-void to_td_outputs(const CompatRun &run, int n, int *S_h, float *sigma_h) {
-  for (int v = 0; v < n; ++v) {
-    S_h[v] = run.S[v] < 0 ? 0 : run.S[v];
-    if (sigma_h) sigma_h[v] = (float)run.sigma[v];
-  }
 }
 
 int td_csc(int *IC_h, int *CP_h, int *S_h, float *sigma_h, int r, int nz, int n, int rep) {
   if (!S_h || !sigma_h) return TBFS_ERR_INVALID_ARG;
-  CompatRun run;
-  int st = compat_run(IC_h, CP_h, false, r, nz, n, rep, true, run);
-  if (st == TBFS_OK) to_td_outputs(run, n, S_h, sigma_h);
-  return st;
+  return compat_run(IC_h, CP_h, false, r, nz, n, rep, K_TD, S_h, sigma_h);
 }
 
 int bu_csc(int *I_h, int *CP_h, int *S_h, int r, int nz, int n, int rep) {
   if (!S_h) return TBFS_ERR_INVALID_ARG;
-  CompatRun run;
-  int st = compat_run(I_h, CP_h, false, r, nz, n, rep, false, run);
-  if (st == TBFS_OK) memcpy(S_h, run.S.data(), (size_t)n * sizeof(int));
-  return st;
+  return compat_run(I_h, CP_h, false, r, nz, n, rep, K_BU, S_h, nullptr);
 }
 
-/* The reference's TDBU drivers keep sigma only for the levels they expand
- * top-down: they stay top-down while the last level held at most
- * 0.001f*n vertices (a float compare, bfsgputdbucsc_sc.cu:112-122) and
- * never switch back, and their bottom-up kernel leaves sigma at 0. */
 int tdbu_csc(int *I_h, int *CP_h, int *S_h, int *sigma_h, int r, int nz, int n, int rep) {
   if (!S_h || !sigma_h) return TBFS_ERR_INVALID_ARG;
-  CompatRun run;
-  int st = compat_run(I_h, CP_h, false, r, nz, n, rep, true, run);
-  if (st != TBFS_OK) return st;
-  std::vector<int64_t> cnt((size_t)run.st.levels + 1, 0);
-  for (int v = 0; v < n; ++v)
-    if (run.S[v] >= 0 && run.S[v] < (int)cnt.size()) cnt[run.S[v]]++;
-  const float thr_td = 0.001f;
-  const float thresh_td = thr_td * (float)n;
-  int last_td = run.st.levels; /* deepest level reached top-down */
-  for (int d = 1; d < run.st.levels; ++d)
-    if ((float)cnt[d] > thresh_td) {
-      last_td = d;
-      break;
-    }
-  for (int v = 0; v < n; ++v) {
-    S_h[v] = run.S[v];
-    const bool td_level = run.S[v] >= 0 && run.S[v] <= last_td;
-    sigma_h[v] = td_level ? (int32_t)(uint32_t)(uint64_t)run.sigma[v] : 0;
-  }
-  return TBFS_OK;
+  return compat_run(I_h, CP_h, false, r, nz, n, rep, K_TDBU, S_h, sigma_h);
 }
 
 }  // namespace
@@ -1017,9 +1111,5 @@ extern "C" int bfs_gpu_tdbu_csc_wa(int *IC_h, int *CP_h, int *S_h, int *sigma_h,
 extern "C" int bfs_gpu_td_cooc_sc(int *I_h, int *J_h, float *sigma_h, int r, int nz, int n,
                                   int repetition) {
   if (!sigma_h) return TBFS_ERR_INVALID_ARG;
-  CompatRun run;
-  int st = compat_run(I_h, J_h, true, r, nz, n, repetition, true, run);
-  if (st == TBFS_OK)
-    for (int v = 0; v < n; ++v) sigma_h[v] = (float)run.sigma[v];
-  return st;
+  return compat_run(I_h, J_h, true, r, nz, n, repetition, K_COOC, nullptr, sigma_h);
 }

@@ -202,8 +202,11 @@ extern "C" tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32
     tbfs_status st = tbfs::ensure_ws(g, W, want_sigma, s);
     if (st != TBFS_OK) return st;
     BatchWS *w = g->batch;
+    /* path counts in 32 bits first: half the bytes per hit; a launch that
+     * meets a count needing more is redone with 64-bit counts */
+    int sigmode = want_sigma ? 2 : 0;
     tbfs::LaunchGeom geom;
-    TRY(tbfs::batch_geometry(g->device, W, want_sigma, &geom), "launch geometry");
+    TRY(tbfs::batch_geometry(g->device, W, sigmode, &geom), "launch geometry");
 
     memcpy(w->roots_host, roots + r0, (size_t)kg * sizeof(int));
     TRY(cudaMemcpyAsync(w->roots_dev, w->roots_host, (size_t)kg * sizeof(int),
@@ -310,8 +313,19 @@ extern "C" tbfs_status tbfs_bfs_batch(tbfs_graph *g, const int32_t *roots, int32
     op.r_maxd = reinterpret_cast<int *>(w->rst + 2 * tbfs::kBatchMaxRoots);
 
     TRY(cudaEventRecord(w->ev0, s), "event");
-    TRY(tbfs::batch_launch(p, W, want_sigma, geom, s), "batch launch");
-    TRY(tbfs::batch_output(op, want_sigma, s), "batch results");
+    TRY(tbfs::batch_launch(p, W, sigmode, geom, s), "batch launch");
+    if (sigmode == 2) {
+      TRY(cudaMemcpyAsync(w->ctl_host, w->ctl, sizeof(tbfs::BatchCtl), cudaMemcpyDeviceToHost, s),
+          "read control block");
+      TRY(cudaStreamSynchronize(s), "batch traversal");
+      if (w->ctl_host->wide && w->ctl_host->status == 0) {
+        sigmode = 1;
+        TRY(tbfs::batch_geometry(g->device, W, sigmode, &geom), "launch geometry");
+        TRY(cudaMemsetAsync(w->ctl, 0, sizeof(tbfs::BatchCtl), s), "clear control block");
+        TRY(tbfs::batch_launch(p, W, sigmode, geom, s), "batch launch");
+      }
+    }
+    TRY(tbfs::batch_output(op, sigmode, s), "batch results");
     TRY(cudaEventRecord(w->ev1, s), "event");
     TRY(cudaMemcpyAsync(w->ctl_host, w->ctl, sizeof(tbfs::BatchCtl), cudaMemcpyDeviceToHost, s),
         "read control block");

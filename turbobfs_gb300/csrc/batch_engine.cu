@@ -189,9 +189,9 @@ __device__ __forceinline__ void group_or(unsigned (&x)[W], unsigned gmask) {
 }
 
 /* found as left by scan_list -> the group's found row in every lane */
-template <int W, bool SIG>
+template <int W, int SIG>
 __device__ __forceinline__ void finish_found(unsigned (&found)[W], const Grp<W> &g) {
-  if constexpr (SIG) {
+  if constexpr (SIG != 0) {
     /* word w holds the bytes of lanes 4w .. 4w+3 */
     const unsigned b = found[0];
 #pragma unroll
@@ -226,15 +226,34 @@ __device__ __forceinline__ void cp_async16_off(unsigned s, const void *g, unsign
       : "memory");
 }
 
-/* the four root-pair chunks of one hit row for a lane of a G-lane group:
- * chunk q from g + 16 G q bytes into shared s + 512 q bytes, if pair q of
- * the lane's byte lm is set */
-template <int G>
-__device__ __forceinline__ void fetch_pairs(unsigned s, const unsigned long long *g, unsigned lm) {
-  cp_async16_off<0, 0>(s, g, lm & 0x03u);
-  cp_async16_off<512, 16 * G>(s, g, lm & 0x0cu);
-  cp_async16_off<1024, 32 * G>(s, g, lm & 0x30u);
-  cp_async16_off<1536, 48 * G>(s, g, lm & 0xc0u);
+/* cp.async of 8 bytes (through L1) */
+template <int SOFF, int GOFF>
+__device__ __forceinline__ void cp_async8_off(unsigned s, const void *g, unsigned pred) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t"
+      "@p cp.async.ca.shared.global [%0+%3], [%1+%4], 8;\n\t}" ::"r"(s),
+      "l"(g), "r"(pred), "n"(SOFF), "n"(GOFF)
+      : "memory");
+}
+
+/* the four root-pair chunks of one hit row for a lane of a G-lane group.
+ * 64-bit counts: chunk q (16 bytes) from g + 16 G q bytes into shared
+ * s + 512 q bytes; 32-bit counts (NR): chunk q (8 bytes) from g + 8 G q
+ * bytes into s + 256 q bytes; each copied if pair q of the lane's byte lm is
+ * set */
+template <int G, bool NR>
+__device__ __forceinline__ void fetch_pairs(unsigned s, const void *g, unsigned lm) {
+  if constexpr (NR) {
+    cp_async8_off<0, 0>(s, g, lm & 0x03u);
+    cp_async8_off<256, 8 * G>(s, g, lm & 0x0cu);
+    cp_async8_off<512, 16 * G>(s, g, lm & 0x30u);
+    cp_async8_off<768, 24 * G>(s, g, lm & 0xc0u);
+  } else {
+    cp_async16_off<0, 0>(s, g, lm & 0x03u);
+    cp_async16_off<512, 16 * G>(s, g, lm & 0x0cu);
+    cp_async16_off<1024, 32 * G>(s, g, lm & 0x30u);
+    cp_async16_off<1536, 48 * G>(s, g, lm & 0xc0u);
+  }
 }
 
 /* wait for this thread's outstanding cp.async copies */
@@ -260,11 +279,23 @@ __device__ __forceinline__ void add1(unsigned long long &a, unsigned long long x
 /* acc[b] += the staged count of bit b of lane mask lm (one hit).  Fast path:
  * ovh collects the high words (bit 31 set once any sum reached 2^63); EXACT:
  * ovm gets the bit of every root whose sum reached 2^63. */
-template <bool EXACT>
-__device__ __forceinline__ void acc_staged(const unsigned long long *slot, unsigned lm,
+template <bool EXACT, bool NR>
+__device__ __forceinline__ void acc_staged(const void *slot_v, unsigned lm,
                                            unsigned long long (&acc)[8], unsigned &ovh,
                                            unsigned &ovm) {
-  if constexpr (!EXACT) {
+  const unsigned long long *slot = reinterpret_cast<const unsigned long long *>(slot_v);
+  if constexpr (NR) {
+    /* 32-bit counts: 8-byte chunks 256 bytes apart; any high word set means
+     * a count that 32 bits cannot hold (the launch is then redone wide) */
+    const unsigned *s32 = reinterpret_cast<const unsigned *>(slot_v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint2 x = *reinterpret_cast<const uint2 *>(s32 + q * 64);
+      if (lm & (1u << (2 * q))) acc[2 * q] += x.x;
+      if (lm & (2u << (2 * q))) acc[2 * q + 1] += x.y;
+      ovh |= (unsigned)(acc[2 * q] >> 32) | (unsigned)(acc[2 * q + 1] >> 32);
+    }
+  } else if constexpr (!EXACT) {
     /* branch-free: every chunk slot is read (a slot not copied this time
      * holds a stale value, which no add takes), the adds are predicated on
      * the root bits, and one OR per pair collects both high words */
@@ -305,7 +336,7 @@ __device__ __forceinline__ void report_overflow(const BatchParams &p, unsigned o
  * row), which keeps seven registers free for the path counts.  With SIG,
  * every lane also adds to acc the path counts of its roots set in F_d[u] &
  * want.  sm: the warp's 32 x W staging words. */
-template <int W, bool SIG, bool EXACT>
+template <int W, int SIG, bool EXACT>
 __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *Fd, int lo, int hi,
                                           const unsigned (&want)[W], unsigned (&found)[W],
                                           unsigned long long (&acc)[8], unsigned &ovh,
@@ -330,7 +361,7 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
 #pragma unroll
       for (int w = 0; w < W; ++w) m[w] = 0u;
     }
-    if constexpr (!SIG) {
+    if constexpr (SIG == 0) {
 #pragma unroll
       for (int w = 0; w < W; ++w) found[w] |= m[w];
     }
@@ -343,7 +374,9 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
         /* kHitBatch hit rows per round trip: every lane copies the chunks of
          * its roots that are set (16 bytes per root pair) into its own stage
          * slots, waits for its own copies only, then accumulates */
-        unsigned long long *mine = sm.stage + g.lane * 2;
+        constexpr bool NR = SIG == 2;
+        constexpr unsigned kHitBytes = NR ? 1024u : 2048u; /* stage bytes of one hit */
+        unsigned char *mine = reinterpret_cast<unsigned char *>(sm.stage) + g.lane * (NR ? 8 : 16);
         const unsigned s_mine = (unsigned)__cvta_generic_to_shared(mine);
         do {
           unsigned lms[kHitBatch];
@@ -357,14 +390,17 @@ __device__ __forceinline__ void scan_list(const BatchParams &p, const unsigned *
               const unsigned lm = lane_bits_smem<W>(sm.m + (g.gbase + j) * W, g);
               lms[b] = lm;
               found[0] |= lm;
-              const unsigned long long *row = p.sig_int + (size_t)uj * RS;
-              fetch_pairs<G>(s_mine + 2048u * (unsigned)b, row + 2 * g.gl, lm);
+              const void *row =
+                  NR ? (const void *)(reinterpret_cast<const unsigned *>(p.sig_int) +
+                                      (size_t)uj * RS + 2 * g.gl)
+                     : (const void *)(p.sig_int + (size_t)uj * RS + 2 * g.gl);
+              fetch_pairs<G, NR>(s_mine + kHitBytes * (unsigned)b, row, lm);
             }
           }
           cp_async_wait_all();
 #pragma unroll
           for (int b = 0; b < kHitBatch; ++b)
-            if (lms[b]) acc_staged<EXACT>(mine + 4 * b * 64, lms[b], acc, ovh, ovm);
+            if (lms[b]) acc_staged<EXACT, NR>(mine + kHitBytes * b, lms[b], acc, ovh, ovm);
         } while (hits);
         __syncwarp(g.gmask);
       }
@@ -383,12 +419,12 @@ __device__ __forceinline__ unsigned exact_overflow(const BatchParams &p, const u
   for (int w = 0; w < W; ++w) f[w] = 0u;
   unsigned long long a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   unsigned oh = 0, om = 0;
-  scan_list<W, true, true>(p, Fd, lo, hi, want, f, a, oh, om, sm, g);
+  scan_list<W, 1, true>(p, Fd, lo, hi, want, f, a, oh, om, sm, g);
   return om;
 }
 
 /* write depth d+1 (and the counts) of the roots of lane mask nb at vertex v */
-template <int W, bool SIG>
+template <int W, int SIG>
 __device__ __forceinline__ void write_new(const BatchParams &p, int d, int v, unsigned nb,
                                           const unsigned long long (&acc)[8], const Grp<W> &g) {
   constexpr int RS = 32 * W;
@@ -399,14 +435,18 @@ __device__ __forceinline__ void write_new(const BatchParams &p, int d, int v, un
     const unsigned pr = (nb >> (2 * q)) & 3u;
     if (!pr) continue;
     const size_t at = (size_t)v * RS + 2 * (g.gl + G * q);
+    unsigned *c32 = reinterpret_cast<unsigned *>(p.sig_int);
     if (pr == 3u) {
       *reinterpret_cast<int2 *>(p.S_int + at) = make_int2(d + 1, d + 1);
-      if (SIG)
+      if (SIG == 2)
+        *reinterpret_cast<uint2 *>(c32 + at) = make_uint2((unsigned)acc[2 * q], (unsigned)acc[2 * q + 1]);
+      else if (SIG)
         *reinterpret_cast<ulonglong2 *>(p.sig_int + at) = make_ulonglong2(acc[2 * q], acc[2 * q + 1]);
     } else {
       const int t = pr == 2u ? 1 : 0;
       p.S_int[at + t] = d + 1;
-      if (SIG) p.sig_int[at + t] = t ? acc[2 * q + 1] : acc[2 * q];
+      if (SIG == 2) c32[at + t] = (unsigned)(t ? acc[2 * q + 1] : acc[2 * q]);
+      else if (SIG) p.sig_int[at + t] = t ? acc[2 * q + 1] : acc[2 * q];
     }
   }
 }
@@ -423,7 +463,7 @@ __device__ __forceinline__ bool row_full(const BatchParams &p, const unsigned (&
 /* ---- per-vertex work ------------------------------------------------------- */
 
 /* pull level, whole in-list of v (not a hub): discover and count */
-template <int W, bool SIG>
+template <int W, int SIG>
 __device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, int lo, int hi,
                                             const unsigned (&sn)[W], const unsigned *Fd,
                                             unsigned *F1, const WarpSmem &sm, const Grp<W> &g,
@@ -444,7 +484,9 @@ __device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, 
   full = false;
   if (!__any_sync(g.gmask, anyf)) return;
   finish_found<W, SIG>(found, g);
-  if (SIG && __any_sync(g.gmask, (ovh >> 31) != 0u)) {
+  if (SIG == 2) {
+    if (__any_sync(g.gmask, ovh != 0u) && g.gl == 0) p.ctl->wide = 1;
+  } else if (SIG && __any_sync(g.gmask, (ovh >> 31) != 0u)) {
     ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
     report_overflow<W>(p, ovm, g);
   }
@@ -467,7 +509,7 @@ __device__ __forceinline__ void pull_vertex(const BatchParams &p, int d, int v, 
 
 /* Fold a segment's partial result into hub h: new bits into F1 (pull only),
  * partial counts into sig_int by atomics.  found must be group-reduced. */
-template <int W, bool SIG, bool DISC>
+template <int W, int SIG, bool DISC>
 __device__ __forceinline__ void commit_segment(const BatchParams &p, int h, const unsigned (&found)[W],
                                                const unsigned long long (&acc)[8], unsigned ovh,
                                                const unsigned *Fd, int lo, int hi,
@@ -478,7 +520,22 @@ __device__ __forceinline__ void commit_segment(const BatchParams &p, int h, cons
     const unsigned fw = pick<W>(found, g.gl);
     if (fw) atomicOr(&F1[(size_t)h * W + g.gl], fw);
   }
-  if (SIG) {
+  if (SIG == 2) { /* 32-bit counts: any count past 32 bits redoes the launch wide */
+    bool wide = __any_sync(g.gmask, ovh != 0u);
+    const unsigned nb = lane_bits<W>(found, g);
+    if (nb) {
+      unsigned *crow = reinterpret_cast<unsigned *>(p.sig_int) + (size_t)h * RS;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        if ((nb >> b) & 1u) {
+          const unsigned x = (unsigned)acc[b];
+          const unsigned old = atomicAdd(crow + g.root(b), x);
+          if (old + x < old) wide = true;
+        }
+      }
+    }
+    if (wide) p.ctl->wide = 1;
+  } else if (SIG) {
     unsigned ovm = 0;
     if (__any_sync(g.gmask, (ovh >> 31) != 0u)) ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
     const unsigned nb = lane_bits<W>(found, g);
@@ -514,7 +571,7 @@ __device__ __forceinline__ bool arrive_last(const BatchParams &p, int h, unsigne
 }
 
 /* pull level, one segment of hub h */
-template <int W, bool SIG>
+template <int W, int SIG>
 __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h, int lo, int hi,
                                              unsigned nseg, const unsigned (&sn)[W],
                                              const unsigned *Fd, unsigned *F1, const WarpSmem &sm,
@@ -559,7 +616,7 @@ __device__ __forceinline__ void pull_segment(const BatchParams &p, int d, int h,
 
 /* push level, second phase: counts of the roots new at v (all of them known
  * now in F1[v]); finishes v (depths, seen, queue-membership bit) */
-template <int W, bool SIG>
+template <int W, int SIG>
 __device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v, int lo, int hi,
                                              const unsigned *Fd, const unsigned *F1, const WarpSmem &sm,
                                              const Grp<W> &g, bool &full) {
@@ -572,8 +629,10 @@ __device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v,
 #pragma unroll
     for (int w = 0; w < W; ++w) found[w] = 0u;
     unsigned ovh = 0, ovm = 0;
-    scan_list<W, true, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
-    if (__any_sync(g.gmask, (ovh >> 31) != 0u)) {
+    scan_list<W, SIG, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
+    if (SIG == 2) {
+      if (__any_sync(g.gmask, ovh != 0u) && g.gl == 0) p.ctl->wide = 1;
+    } else if (__any_sync(g.gmask, (ovh >> 31) != 0u)) {
       ovm = exact_overflow<W>(p, Fd, lo, hi, want, sm, g);
       report_overflow<W>(p, ovm, g);
     }
@@ -588,7 +647,7 @@ __device__ __forceinline__ void count_vertex(const BatchParams &p, int d, int v,
 }
 
 /* push level, second phase, one segment of hub h (path counts only) */
-template <int W>
+template <int W, int SIG>
 __device__ __forceinline__ void count_segment(const BatchParams &p, int d, int h, int lo, int hi,
                                               unsigned nseg, const unsigned *Fd, unsigned *F1,
                                               const WarpSmem &sm, const Grp<W> &g, bool &full) {
@@ -598,13 +657,13 @@ __device__ __forceinline__ void count_segment(const BatchParams &p, int d, int h
   for (int w = 0; w < W; ++w) found[w] = 0u;
   unsigned long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   unsigned ovh = 0, ovm = 0;
-  scan_list<W, true, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
+  scan_list<W, SIG, false>(p, Fd, lo, hi, want, found, acc, ovh, ovm, sm, g);
   bool anyf = false;
 #pragma unroll
   for (int w = 0; w < W; ++w) anyf |= found[w] != 0u;
   if (__any_sync(g.gmask, anyf)) {
-    finish_found<W, true>(found, g);
-    commit_segment<W, true, false>(p, h, found, acc, ovh, Fd, lo, hi, want, F1, sm, g);
+    finish_found<W, SIG>(found, g);
+    commit_segment<W, SIG, false>(p, h, found, acc, ovh, Fd, lo, hi, want, F1, sm, g);
   }
   full = false;
   if (!arrive_last<W>(p, h, nseg, g)) return;
@@ -694,7 +753,7 @@ __device__ __forceinline__ unsigned upper_owner(const T *pre, unsigned cnt, unsi
 #define TBFS_BATCH_MINB 3 /* 3 CTAs of 256 per SM: 24 warps hide more latency than 128 registers would save */
 #endif
 
-template <int W, bool SIG>
+template <int W, int SIG>
 __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const BatchParams p) {
   constexpr int PER = Grp<W>::PER_WARP;
   constexpr int RS = 32 * W;
@@ -721,7 +780,10 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
   }
   for (long long i = tid; i < ((long long)n + 31) / 32; i += nth) p.touched[i] = 0u;
   for (long long i = tid; i < n; i += nth) p.seg_arrive[i] = 0u;
-  if (SIG) {
+  if (SIG == 2) {
+    for (long long i = tid; i < (long long)p.nhub * RS; i += nth)
+      reinterpret_cast<unsigned *>(p.sig_int)[(size_t)__ldg(p.hubs + i / RS) * RS + i % RS] = 0u;
+  } else if (SIG) {
     for (long long i = tid; i < (long long)p.nhub * RS; i += nth)
       p.sig_int[(size_t)__ldg(p.hubs + i / RS) * RS + i % RS] = 0ull;
   }
@@ -740,7 +802,8 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
       atomicOr(&p.seen[(size_t)v * W + (b >> 5)], 1u << (b & 31));
       atomicOr(&p.F[0][(size_t)v * W + (b >> 5)], 1u << (b & 31));
       p.S_int[(size_t)v * RS + t] = 0;
-      if (SIG) p.sig_int[(size_t)v * RS + t] = 1ull;
+      if (SIG == 2) reinterpret_cast<unsigned *>(p.sig_int)[(size_t)v * RS + t] = 1u;
+      else if (SIG) p.sig_int[(size_t)v * RS + t] = 1ull;
     }
     s_rv[t] = v;
     __syncthreads();
@@ -945,7 +1008,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
             }
             if (g.gl == 0 && full) md += (unsigned long long)deg;
           }
-        } else if constexpr (SIG) {
+        } else if constexpr (SIG != 0) {
           const unsigned s = (it - nA2) * PER + g.gid;
           bool full = false;
           int deg = 0;
@@ -957,7 +1020,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
             deg = ch - cl;
             const int lo = cl + (int)si * p.seg_len;
             const int hi = min(ch, lo + p.seg_len);
-            count_segment<W>(p, d, h, lo, hi, nsegs(deg, p.seg_len), Fd, F1, sm, g, full);
+            count_segment<W, SIG>(p, d, h, lo, hi, nsegs(deg, p.seg_len), Fd, F1, sm, g, full);
           }
           if (g.gl == 0 && full) md += (unsigned long long)deg;
         }
@@ -1070,7 +1133,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
 
 /* ---- results: internal rows -> caller layout, per-root statistics ---------- */
 
-template <int W, bool SIG>
+template <int W, int SIG>
 __global__ void __launch_bounds__(256) fm_output_kernel(const BatchOutParams o) {
   constexpr int RS = 32 * W;
   __shared__ int sS[32][33];
@@ -1096,7 +1159,8 @@ __global__ void __launch_bounds__(256) fm_output_kernel(const BatchOutParams o) 
         const unsigned sw = __ldg(o.seen + (size_t)v * W + (rbit >> 5));
         if (rv && ((sw >> (rbit & 31)) & 1u)) {
           s = __ldg(o.S_int + (size_t)v * RS + r);
-          if (SIG) cv = __ldg(o.sig_int + (size_t)v * RS + r);
+          if (SIG == 2) cv = __ldg(reinterpret_cast<const unsigned *>(o.sig_int) + (size_t)v * RS + r);
+          else if (SIG) cv = __ldg(o.sig_int + (size_t)v * RS + r);
           ++vis;
           edg += (unsigned long long)(__ldg(o.rp + v + 1) - __ldg(o.rp + v));
           mdep = max(mdep, s);
@@ -1161,22 +1225,27 @@ __global__ void hub_fill_kernel(const int *cp, int n, int seg_len, const int *po
   }
 }
 
-template <int W, bool SIG>
-const void *kernel_of() {
-  return reinterpret_cast<const void *>(fm_bfs_kernel<W, SIG>);
+template <int W>
+const void *kernel_of(int sigma) {
+  switch (sigma) {
+    case 0: return reinterpret_cast<const void *>(fm_bfs_kernel<W, 0>);
+    case 1: return reinterpret_cast<const void *>(fm_bfs_kernel<W, 1>);
+    case 2: return reinterpret_cast<const void *>(fm_bfs_kernel<W, 2>);
+    default: return nullptr;
+  }
 }
 
 /* dynamic shared memory of the kernel: the path-count stage */
-size_t stage_bytes(bool sigma) {
+size_t stage_bytes(int sigma) {
   return sigma ? (size_t)kWarps * kStageU64 * sizeof(unsigned long long) : 0;
 }
 
-const void *batch_kernel(int W, bool sigma) {
+const void *batch_kernel(int W, int sigma) {
   switch (W) {
-    case 1: return sigma ? kernel_of<1, true>() : kernel_of<1, false>();
-    case 2: return sigma ? kernel_of<2, true>() : kernel_of<2, false>();
-    case 4: return sigma ? kernel_of<4, true>() : kernel_of<4, false>();
-    case 8: return sigma ? kernel_of<8, true>() : kernel_of<8, false>();
+    case 1: return kernel_of<1>(sigma);
+    case 2: return kernel_of<2>(sigma);
+    case 4: return kernel_of<4>(sigma);
+    case 8: return kernel_of<8>(sigma);
     default: return nullptr;
   }
 }
@@ -1222,7 +1291,7 @@ cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_
   return cudaSuccess;
 }
 
-cudaError_t batch_geometry(int device, int W, bool sigma, LaunchGeom *out) {
+cudaError_t batch_geometry(int device, int W, int sigma, LaunchGeom *out) {
   const void *k = batch_kernel(W, sigma);
   if (!k) return cudaErrorInvalidValue;
   int sms = 0, coop = 0, per = 0;
@@ -1244,7 +1313,7 @@ cudaError_t batch_geometry(int device, int W, bool sigma, LaunchGeom *out) {
   return cudaSuccess;
 }
 
-cudaError_t batch_launch(const BatchParams &p, int W, bool sigma, const LaunchGeom &g,
+cudaError_t batch_launch(const BatchParams &p, int W, int sigma, const LaunchGeom &g,
                          cudaStream_t s) {
   const void *k = batch_kernel(W, sigma);
   if (!k) return cudaErrorInvalidValue;
@@ -1252,26 +1321,21 @@ cudaError_t batch_launch(const BatchParams &p, int W, bool sigma, const LaunchGe
   return cudaLaunchCooperativeKernel(k, dim3(g.grid), dim3(g.block), args, stage_bytes(sigma), s);
 }
 
-cudaError_t batch_output(const BatchOutParams &o, bool sigma, cudaStream_t s) {
+template <int W>
+void output_w(const BatchOutParams &o, int sigma, dim3 grid, cudaStream_t s) {
+  if (sigma == 2) fm_output_kernel<W, 2><<<grid, 256, 0, s>>>(o);
+  else if (sigma == 1) fm_output_kernel<W, 1><<<grid, 256, 0, s>>>(o);
+  else fm_output_kernel<W, 0><<<grid, 256, 0, s>>>(o);
+}
+
+cudaError_t batch_output(const BatchOutParams &o, int sigma, cudaStream_t s) {
   const int ntiles = (o.n + 31) / 32;
   const dim3 grid((unsigned)min(ntiles, 4096), (unsigned)((o.k + 31) / 32));
   switch (o.W) {
-    case 1:
-      sigma ? fm_output_kernel<1, true><<<grid, 256, 0, s>>>(o)
-            : fm_output_kernel<1, false><<<grid, 256, 0, s>>>(o);
-      break;
-    case 2:
-      sigma ? fm_output_kernel<2, true><<<grid, 256, 0, s>>>(o)
-            : fm_output_kernel<2, false><<<grid, 256, 0, s>>>(o);
-      break;
-    case 4:
-      sigma ? fm_output_kernel<4, true><<<grid, 256, 0, s>>>(o)
-            : fm_output_kernel<4, false><<<grid, 256, 0, s>>>(o);
-      break;
-    case 8:
-      sigma ? fm_output_kernel<8, true><<<grid, 256, 0, s>>>(o)
-            : fm_output_kernel<8, false><<<grid, 256, 0, s>>>(o);
-      break;
+    case 1: output_w<1>(o, sigma, grid, s); break;
+    case 2: output_w<2>(o, sigma, grid, s); break;
+    case 4: output_w<4>(o, sigma, grid, s); break;
+    case 8: output_w<8>(o, sigma, grid, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

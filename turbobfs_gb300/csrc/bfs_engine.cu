@@ -682,10 +682,20 @@ cudaError_t bfs_geometry(int device, LaunchGeom *out) {
   e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
   if (e != cudaSuccess) return e;
   if (!coop) return cudaErrorNotSupported;
-  /* the kernel needs ~20 KB of shared memory per CTA; leave the rest of the
-   * unified L1/shared array to L1, which caches the depth/path-count gathers */
+  /* the kernel needs ~20 KB of shared memory per CTA: carve out just enough
+   * for TBFS_MIN_BLOCKS CTAs and leave the rest of the unified L1/shared
+   * array to L1, which caches the depth/path-count gathers */
+  int smem_sm = 0;
+  e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, bfs_persistent_kernel);
+  if (e != cudaSuccess) return e;
+  const size_t need = (size_t)TBFS_MIN_BLOCKS * (fa.sharedSizeBytes + 1024);
+  int carve = (int)((100 * need + (size_t)smem_sm - 1) / (size_t)smem_sm);
+  carve = carve < 100 ? carve : 100;
   e = cudaFuncSetAttribute(bfs_persistent_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           25);
+                           carve);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bfs_persistent_kernel, kBlock, 0);
   if (e != cudaSuccess) return e;

@@ -5,6 +5,7 @@
  *                        for COOC -> CSC (key = column) and for the transpose
  *                        CSC -> out-lists (key = row id)
  *   expand_columns       column id of every CSC entry
+ *   symmetric_check      whether the CSC equals its transpose (keyed multiset hash)
  *   stable_sort_pairs    LSD radix sort of (key, val) pairs, 8 bits a pass,
  *                        stable: equal keys keep their input order
  * Replaces the host-side format builders of the reference
@@ -16,6 +17,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "device_common.cuh"
 #include "tbfs_internal.h"
 
 namespace tbfs {
@@ -52,6 +54,46 @@ __global__ void histogram_kernel(const int *keys, long long nnz, int n, int *cnt
       continue;
     }
     atomicAdd(cnt + key, 1);
+  }
+}
+
+/* SplitMix64's output function (S. Vigna; a bijection of 64-bit words) */
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+/* Sum over the entries u -> v (u in column v) of h(u, v) - h(v, u), for two
+ * keyed hashes h_k(x, y) = mix64(((x << 32) | y) ^ k), modulo 2^64.  A
+ * warp takes chunks of kSymChunk consecutive entries; a lane follows its
+ * entries' columns along col_ptr. */
+constexpr int kSymChunk = 4096;
+__global__ void symmetric_hash_kernel(const int *cp, const int *ic, int n, long long nnz,
+                                      unsigned long long k1, unsigned long long k2,
+                                      unsigned long long *out) {
+  const unsigned lane = threadIdx.x & 31;
+  const long long nchunks = (nnz + kSymChunk - 1) / kSymChunk;
+  unsigned long long d1 = 0, d2 = 0;
+  for (long long c = gtid() >> 5; c < nchunks; c += gstride() >> 5) {
+    const long long e0 = c * kSymChunk;
+    const long long e1 = e0 + kSymChunk < nnz ? e0 + kSymChunk : nnz;
+    int col = (int)dev::warp_find_owner(cp, (unsigned)n, (unsigned)e0);
+    for (long long k = e0 + lane; k < e1; k += 32) {
+      while ((long long)__ldg(cp + col + 1) <= k) ++col;
+      const unsigned long long u = (unsigned)__ldg(ic + k), v = (unsigned)col;
+      const unsigned long long a = (u << 32) | v, b = (v << 32) | u;
+      d1 += mix64(a ^ k1) - mix64(b ^ k1);
+      d2 += mix64(a ^ k2) - mix64(b ^ k2);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+    d2 += __shfl_xor_sync(0xffffffffu, d2, o);
+  }
+  if (lane == 0 && (d1 | d2)) {
+    atomicAdd(out, d1);
+    atomicAdd(out + 1, d2);
   }
 }
 
@@ -332,6 +374,28 @@ cudaError_t counting_sort_lists(const int *keys, const int *vals, long long nnz,
   cudaError_t e2 = cudaStreamSynchronize(s);
   tbfs::dev_free(buf);
   return e != cudaSuccess ? e : e2;
+}
+
+cudaError_t symmetric_check(const int *cp, const int *ic, int n, long long nnz,
+                            unsigned long long key1, unsigned long long key2, bool *symmetric,
+                            cudaStream_t s) {
+  *symmetric = false;
+  unsigned long long *acc = nullptr, h[2] = {0, 0};
+  cudaError_t e = tbfs::dev_alloc(&acc, 2 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess && nnz > 0) {
+    const long long warps = (nnz + kSymChunk - 1) / kSymChunk;
+    const long long blocks = (warps * 32 + kThreads - 1) / kThreads;
+    symmetric_hash_kernel<<<(unsigned)(blocks < 4864 ? blocks : 4864), kThreads, 0, s>>>(
+        cp, ic, n, nnz, key1, key2, acc);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, acc, sizeof h, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  tbfs::dev_free(acc);
+  if (e == cudaSuccess) *symmetric = h[0] == 0 && h[1] == 0;
+  return e;
 }
 
 cudaError_t expand_columns(const int *cp, int n, int *col_of_entry, cudaStream_t s) {

@@ -124,7 +124,7 @@ struct __align__(128) BatchCtl {
   unsigned work[4];           /* dynamic work counter of phase ph in work[ph % 4] */
   int status, timeout_level;
   int levels, push_levels, pull_levels;
-  int pad0;
+  int wide; /* a launch with 32-bit counts met a count that needs more bits */
   unsigned ovf[8]; /* bit r: a path count of root r reached 2^63 */
   unsigned pad1[2];
   GridBarrier bar;
@@ -147,7 +147,8 @@ struct BatchParams {
   unsigned *touched;  /* [ceil(n/32)] queue membership during push levels */
   unsigned *seg_arrive; /* [n] cumulative segment arrivals (hubs)         */
   int *S_int;         /* [n][32W] depth of v from root r (valid where seen) */
-  unsigned long long *sig_int; /* [n][32W] path counts, or null            */
+  unsigned long long *sig_int; /* [n][32W] path counts (uint64; uint32 in the
+                                  kernels with 32-bit counts), or null        */
   const int *hubs;    /* vertices with more than seg_len in-list entries   */
   const int *hub_seg; /* exclusive prefix of their segment counts (nhub+1) */
   int nhub;
@@ -181,10 +182,13 @@ struct BatchOutParams {
  * (nhub + 1, exclusive prefix of ceil(indeg / seg_len)), allocated here. */
 cudaError_t batch_hubs(const int *cp, int n, int seg_len, int **hubs, int **hub_seg, int *nhub,
                        int *hub_segs, cudaStream_t s);
-cudaError_t batch_geometry(int device, int W, bool sigma, LaunchGeom *out);
-cudaError_t batch_launch(const BatchParams &p, int W, bool sigma, const LaunchGeom &g,
+/* sigma: 0 depths only, 1 64-bit path counts, 2 32-bit path counts (the
+ * launch sets ctl->wide when a count needs more bits; it is then redone
+ * with 1) */
+cudaError_t batch_geometry(int device, int W, int sigma, LaunchGeom *out);
+cudaError_t batch_launch(const BatchParams &p, int W, int sigma, const LaunchGeom &g,
                          cudaStream_t s);
-cudaError_t batch_output(const BatchOutParams &o, bool sigma, cudaStream_t s);
+cudaError_t batch_output(const BatchOutParams &o, int sigma, cudaStream_t s);
 
 struct BatchWS; /* per-graph batch workspace (batch_api.cu) */
 void batch_ws_free(BatchWS *ws);
@@ -281,6 +285,14 @@ long long scan_partials(long long len);
 cudaError_t exclusive_scan_ws(const int *in, long long len, int *out, int *partial,
                               cudaStream_t s);
 cudaError_t expand_columns(const int *cp, int n, int *col_of_entry, cudaStream_t s);
+/* Whether the CSC (validated) equals its transpose as a multiset of entries:
+ * the sums over all entries u -> v of h(u, v) - h(v, u) vanish for two
+ * keyed 64-bit hashes (keys chosen by the caller at random).  A graph that
+ * is its own transpose always passes; any other passes only when both
+ * independent sums cancel by chance (about 2^-128 for random keys). */
+cudaError_t symmetric_check(const int *cp, const int *ic, int n, long long nnz,
+                            unsigned long long key1, unsigned long long key2, bool *symmetric,
+                            cudaStream_t s);
 /* Degree-based grouping of the vertices (see graph_ingest.cu).  On return
  * *identity tells whether the order is unchanged (then perm/inv/cp2/ic2 are
  * untouched); otherwise perm[new] = old, inv[old] = new and (cp2, ic2) is the
@@ -304,6 +316,9 @@ struct tbfs_graph {
   int *queues = nullptr; /* one allocation: q[3], e[3], a[3], n ints each */
   char *hot = nullptr;   /* one allocation: sigma_work, S_work, bitmaps */
   int deg_bits = 0;      /* bits of the largest in-degree */
+  /* the caller's TBFS_GRAPH_SYMMETRIC (flags may also carry it when the
+   * lists were found to equal their transpose on upload) */
+  bool declared_symmetric = false;
   unsigned *bitmaps = nullptr; /* four frontier bitmaps, (n+31)/32 words each */
   /* degree-grouped numbering: inv[caller id] = internal id (null: identity);
    * the traversal works on internal S/sigma and un-permutes at the end */

@@ -228,7 +228,9 @@ extern "C" tbfs_status tbfs_graph_degree_stats(tbfs_graph *g, int32_t kind,
   out->argmax = -1;
   const int n = g->n;
   if (n == 0) return TBFS_OK;
-  const bool sym = !g->separate_out;
+  /* degree_ug's out + in counts each entry of a declared-undirected graph
+   * once (the file holds one triangle), of any other graph at both ends */
+  const bool sym = g->declared_symmetric;
   const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, 1216);
   cudaError_t e = cudaSetDevice(g->device);
   unsigned long long *dsum = nullptr, *hist = nullptr;
