@@ -67,7 +67,7 @@
 #define TBFS_BLOCK 256
 #endif
 #ifndef TBFS_MIN_BLOCKS
-#define TBFS_MIN_BLOCKS 3 /* 3 CTAs of 256 per SM: 80 registers, no spills */
+#define TBFS_MIN_BLOCKS 4 /* 4 CTAs of 256 per SM: 64 registers (a small spill) */
 #endif
 #ifndef TBFS_RED_PUSH
 #define TBFS_RED_PUSH 1 /* pushes without the overflow check where a bound rules overflow out */
