@@ -179,6 +179,49 @@ def test_native_directed_random_vs_exact(gpu_available):
                 _exact_check(h.col_ptr, h.row_idx, r, res)
 
 
+def _out_degree_graph(n, max_out, seed, hub_out=0):
+    """Directed graph whose vertices have out-degree uniform in [0, max_out]
+    (vertex 1 gets hub_out out-edges when given)."""
+    rng = np.random.default_rng(seed)
+    deg = rng.integers(0, max_out + 1, n)
+    if hub_out:
+        deg[1] = hub_out
+    src = np.repeat(np.arange(n, dtype=np.int32), deg)
+    dst = rng.integers(0, n, src.size, dtype=np.int32)
+    return graphs.from_edges(n, src, dst)
+
+
+@pytest.mark.parametrize("max_out,hub_out", [(16, 0), (16, 17), (3, 0)])
+def test_short_list_levels_vs_exact(gpu_available, max_out, hub_out):
+    """Graphs whose out-lists are all at most 16 entries long expand their
+    small top-down levels in entry-aligned items (no owner search); one list
+    of 17 entries switches the graph to the general instance.  Both equal the
+    exact oracle, with path counts, in every mode, from several roots."""
+    h = _out_degree_graph(30000, max_out, seed=max_out + hub_out, hub_out=hub_out)
+    with tb.Graph.from_host_csc(h) as g:
+        for r in (0, 1, 777, 29999):
+            for mode in MODES:
+                _exact_check(h.col_ptr, h.row_idx, r, g.bfs(r, mode=mode))
+                if mode == "td":
+                    _exact_check(h.col_ptr, h.row_idx, r, g.bfs(r, mode=mode, sigma=False),
+                                 want_sigma=False)
+
+
+def test_short_list_deep_ladder_vs_exact(gpu_available):
+    """A 2 x 20000 ladder (20000 levels of two vertices, out-degree <= 3)
+    and the same ladder directed one way: every level is a short one."""
+    n2 = 20000
+    a = np.arange(n2 - 1, dtype=np.int32)
+    src = np.concatenate([a, a + n2, np.arange(n2, dtype=np.int32)])
+    dst = np.concatenate([a + 1, a + 1 + n2, np.arange(n2, dtype=np.int32) + n2])
+    for sym in (True, False):
+        h = graphs.from_edges(2 * n2, src, dst, symmetrize=sym)
+        with tb.Graph.from_host_csc(h) as g:
+            for r in (0, n2 + 5000):
+                res = g.bfs(r)
+                _exact_check(h.col_ptr, h.row_idx, r, res)
+
+
 def test_bfs_many_matches_single(gpu_available):
     h = graphs.rmat(14, 16, seed=9)
     roots = graphs.pick_roots(h, 6, seed=2)

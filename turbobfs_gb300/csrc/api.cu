@@ -175,6 +175,12 @@ static tbfs_status graph_finish(tbfs_graph *g) {
     int b = 0;
     while (b < 63 && (1ll << b) <= maxd) ++b; /* maxd < 2^b */
     g->deg_bits = b;
+    int max_out = (int)maxd;
+    if (g->separate_out) {
+      cudaError_t e = tbfs::longest_list(g->rp, g->n, &max_out);
+      if (e != cudaSuccess) return cuda_fail(e, "out-degree bound", __LINE__);
+    }
+    g->short_lists = max_out <= tbfs::kShortList;
   }
   return TBFS_OK;
 }
@@ -677,6 +683,7 @@ static BfsParams make_params(tbfs_graph *g, int32_t root, const tbfs_options &o,
   p.max_ept = o.max_ept;
   p.ctas_per_sm = o.ctas_per_sm;
   p.deg_bits = g->deg_bits;
+  p.short_lists = g->short_lists ? 1 : 0;
   return p;
 }
 

@@ -69,6 +69,12 @@
 #ifndef TBFS_MIN_BLOCKS
 #define TBFS_MIN_BLOCKS 4 /* 4 CTAs of 256 per SM: 64 registers (a small spill) */
 #endif
+#ifndef TBFS_SHORT_LEVELS
+#define TBFS_SHORT_LEVELS 1 /* small top-down levels of short-list graphs: a queue entry per lane */
+#endif
+#ifndef TBFS_SPREAD_ITEMS
+#define TBFS_SPREAD_ITEMS 1 /* static work items round-robin over the CTAs */
+#endif
 #ifndef TBFS_RED_PUSH
 #define TBFS_RED_PUSH 1 /* pushes without the overflow check where a bound rules overflow out */
 #endif
@@ -86,6 +92,9 @@ constexpr int kBlock = TBFS_BLOCK;
 constexpr int kWarps = kBlock / 32;
 constexpr int kWin = 128;          /* queue entries staged per warp window */
 constexpr int kEPT = TBFS_EPT;     /* most consecutive edges per lane/round */
+/* queue entries per item of a small level of a short-list graph: at most
+ * 8 * kShortList = 128 edges, one round of at most 4 per lane */
+constexpr unsigned kShortEntries = 8;
 constexpr double kBuWordCost = 4.0; /* a bitmap word of a bottom-up level, in list entries */
 enum { DIR_TD = 0, DIR_BU = 1 };
 
@@ -178,16 +187,22 @@ __device__ __forceinline__ bool bit_of(const unsigned *bm, int v) {
  * targets).  Without DISC, membership of a neighbour in the level the mode
  * needs (d-1 for PULL, tgt for PUSH_AT) is read from bitmap tb, one bit per
  * vertex, instead of from S. */
-template <bool DISC, int SIG, bool CHK = true>
+template <bool DISC, int SIG, bool CHK = true, bool ALIGNED = false>
 __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt, const Queue &Q,
                                              unsigned E0, unsigned E1, unsigned ept,
                                              const NextQueue &nx, const unsigned *tb,
-                                             unsigned *nb, WarpWin &w, bool &ovf) {
+                                             unsigned *nb, WarpWin &w, bool &ovf,
+                                             unsigned first = 0, unsigned count = 0) {
   const int lane = threadIdx.x & 31;
-  unsigned i0 = warp_find_owner(Q.e, Q.qn, E0);
+  /* ALIGNED item: entries [first, first + count), all their edges, one
+   * window; E0 = 0 and E1 = ~0u, so the window offsets below are the
+   * entries' own edge offsets and no owner search is needed */
+  constexpr bool aligned = ALIGNED;
+  unsigned i0 = aligned ? first : warp_find_owner(Q.e, Q.qn, E0);
   unsigned pos = E0;
   while (pos < E1 && i0 < Q.qn) {
-    const unsigned nw = (Q.qn - i0) < (unsigned)kWin ? (Q.qn - i0) : (unsigned)kWin;
+    unsigned nw = (Q.qn - i0) < (unsigned)kWin ? (Q.qn - i0) : (unsigned)kWin;
+    if (aligned && count < nw) nw = count;
     for (unsigned k = lane; k < nw; k += 32) {
       const unsigned i = i0 + k;
       const unsigned eb = (unsigned)__ldcg(Q.e + i);
@@ -201,7 +216,7 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
         w.lo[k] = 0u;
         w.hi[k] = 0u;
       }
-      if (SIG == SIG_PUSH_NEW || SIG == SIG_PUSH_AT) {
+      if ((SIG == SIG_PUSH_NEW || SIG == SIG_PUSH_AT) && !aligned) {
         const unsigned long long x = p.sigma[v];
         w.lo[k] = (unsigned)x;
         w.hi[k] = (unsigned)(x >> 32);
@@ -212,9 +227,15 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
       w.s[nw] = (ee < E1 ? ee : E1) - pos;
     }
     __syncwarp();
-    const unsigned tot = w.s[nw];
+    /* window edges t in [s[0], s[nw]): s[0] = 0 for an edge chunk, the
+     * first entry's edge offset for an entry-aligned item */
+    const unsigned t_beg = aligned ? w.s[0] : 0u, tot = w.s[nw];
+    if (aligned) { /* one round when it fits: (edges + 31) / 32 per lane */
+      const unsigned per = (tot - t_beg + 31u) / 32u;
+      ept = per < 1u ? 1u : (per > ept ? ept : per);
+    }
     const unsigned round = 32u * ept;
-    for (unsigned base = 0; base < tot; base += round) {
+    for (unsigned base = t_beg; base < tot; base += round) {
       const unsigned t0 = base + (unsigned)lane * ept;
       const unsigned tend = t0 + ept < tot ? t0 + ept : tot;
       int u[kEPT], kk[kEPT];
@@ -246,6 +267,13 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
 #pragma unroll
       for (int j = 0; j < kEPT; ++j) /* list reads, all in flight */
         if ((valid >> j) & 1u) u[j] = __ldg(p.jr + u[j]);
+      /* an aligned item reads its entries' path counts with the list
+       * entries instead of staging them first: one round trip fewer */
+      unsigned long long xs[kEPT];
+      if (aligned && SIG == SIG_PUSH_NEW) {
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) xs[j] = ((valid >> j) & 1u) ? p.sigma[w.v[kk[j]]] : 0ull;
+      }
       int su[kEPT];   /* DISC: depth of the neighbour                        */
       unsigned in = 0; /* bit j: neighbour j is in the level the sigma mode needs */
       if (DISC) {
@@ -300,7 +328,9 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
           const bool add = SIG == SIG_PUSH_NEW ? ((hit >> j) & 1u) != 0 : ((in >> j) & 1u) != 0;
           if (add) {
             const unsigned long long x =
-                ((unsigned long long)w.hi[kk[j]] << 32) | (unsigned long long)w.lo[kk[j]];
+                aligned && SIG == SIG_PUSH_NEW
+                    ? xs[j]
+                    : ((unsigned long long)w.hi[kk[j]] << 32) | (unsigned long long)w.lo[kk[j]];
             if (CHK) add_chk(atomicAdd(p.sigma + u[j], x), x, ovf);
             else atomicAdd(p.sigma + u[j], x); /* result unused: a reduction, no round trip */
           }
@@ -332,6 +362,7 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
       }
     }
     __syncwarp();
+    if (aligned) break;
     pos += tot;
     i0 += nw;
   }
@@ -412,6 +443,23 @@ __device__ __forceinline__ void run_expand_item(const BfsParams &p, int d, const
   }
 }
 
+/* One item of a small top-down level of a short-list graph: queue entries
+ * [first, first + kShortEntries) with all their edges (ALIGNED expand_chunk:
+ * no owner search). */
+__device__ __forceinline__ void run_short_item(const BfsParams &p, int d, const ExpandTask &t, unsigned first,
+                    unsigned max_ept, const NextQueue &nx, unsigned *nb, WarpWin &w, bool &ovf) {
+  const unsigned ept = max_ept < 4u ? max_ept : 4u;
+  if (t.kind == EX_DISC)
+    expand_chunk<true, SIG_NONE, true, true>(p, d, 0, t.Q, 0u, ~0u, ept, nx, t.tb, nb, w, ovf,
+                                             first, kShortEntries);
+  else if (t.chk)
+    expand_chunk<true, SIG_PUSH_NEW, true, true>(p, d, 0, t.Q, 0u, ~0u, ept, nx, t.tb, nb, w,
+                                                 ovf, first, kShortEntries);
+  else
+    expand_chunk<true, SIG_PUSH_NEW, false, true>(p, d, 0, t.Q, 0u, ~0u, ept, nx, t.tb, nb, w,
+                                                  ovf, first, kShortEntries);
+}
+
 /* Bottom-up discovery.  A warp takes kBuWords consecutive 32-vertex words
  * per iteration; lane i owns vertex 32*word+i of each, so the depth checks,
  * list bounds and the first gathers of all kBuWords vertices are in flight
@@ -484,6 +532,7 @@ __device__ void bu_tile(const BfsParams &p, int d, const NextQueue &nx, const un
   }
 }
 
+template <bool SHORT>
 __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel(const BfsParams p) {
   __shared__ WarpWin s_win[kWarps];
   WarpWin &win = s_win[threadIdx.x >> 5];
@@ -531,6 +580,8 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
   int sig_bits = 1;
   for (;;) {
     const unsigned long long cur = __ldcg(&ctl->qctr[d % 3]);
+    /* read with the counter, so that both loads are in flight together */
+    const bool ovf_seen = TBFS_RED_PUSH && want_sigma && __ldcg(&ctl->sigma_overflow) != 0;
     const unsigned qn = (unsigned)(cur >> 32);
     const unsigned qe = (unsigned)cur;
     if (qn == 0) {
@@ -608,7 +659,6 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     const unsigned max_ept =
         p.max_ept > 0 && p.max_ept < kEPT ? (unsigned)p.max_ept : (unsigned)kEPT;
     if (TBFS_RED_PUSH && want_sigma) {
-      const bool ovf_seen = dev::ld_volatile(&ctl->sigma_overflow) != 0;
       const int nb_next = sig_bits + p.deg_bits; /* bound of F_{d+1} */
       if (A.kind == EX_DISC_PUSH_NEW)
         A.chk = !ovf_seen && !(p.deg_bits > 0 && nb_next <= 63);
@@ -623,7 +673,21 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     /* work items: the first statically (global warp index), the rest from
      * the level's counter past the static range, so that a small level
      * costs no same-address atomics */
-    unsigned item = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    /* static items go round-robin over the CTAs (item i to CTA i % grid),
+     * so that a small level's work spreads over as many SMs as it has
+     * items instead of filling the first CTAs' warps */
+    unsigned item = TBFS_SPREAD_ITEMS ? (threadIdx.x >> 5) * gridDim.x + blockIdx.x
+                                      : blockIdx.x * kWarps + (threadIdx.x >> 5);
+    /* a small top-down level of a graph with short lists: items of
+     * kShortEntries queue entries each, no owner search (expand_chunk) */
+    const bool short_level = SHORT && B.kind == EX_NONE &&
+                             (A.kind == EX_DISC || A.kind == EX_DISC_PUSH_NEW) &&
+                             qn <= kShortEntries * nwarps;
+    if (short_level) {
+      const unsigned first = item * kShortEntries;
+      if (first < qn) run_short_item(p, d, A, first, max_ept, nx, bm_next, win, ovf);
+      item = n_all; /* done */
+    }
     while (item < n_all) {
       if (item < n_a) run_expand_item(p, d, A, item, nx, bm_next, win, ovf);
       else if (item < n_ab) run_expand_item(p, d, B, item - n_a, nx, bm_next, win, ovf);
@@ -688,17 +752,24 @@ cudaError_t bfs_geometry(int device, LaunchGeom *out) {
   int smem_sm = 0;
   e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
   if (e != cudaSuccess) return e;
-  cudaFuncAttributes fa;
-  e = cudaFuncGetAttributes(&fa, bfs_persistent_kernel);
-  if (e != cudaSuccess) return e;
-  const size_t need = (size_t)TBFS_MIN_BLOCKS * (fa.sharedSizeBytes + 1024);
-  int carve = (int)((100 * need + (size_t)smem_sm - 1) / (size_t)smem_sm);
-  carve = carve < 100 ? carve : 100;
-  e = cudaFuncSetAttribute(bfs_persistent_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                           carve);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bfs_persistent_kernel, kBlock, 0);
-  if (e != cudaSuccess) return e;
+  /* both instances (with and without the short-list levels) have the same
+   * shared memory and register bound; the launch takes the smaller fit */
+  per = 1 << 30;
+  for (const void *fn : {reinterpret_cast<const void *>(bfs_persistent_kernel<false>),
+                         reinterpret_cast<const void *>(bfs_persistent_kernel<true>)}) {
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, fn);
+    if (e != cudaSuccess) return e;
+    const size_t need = (size_t)TBFS_MIN_BLOCKS * (fa.sharedSizeBytes + 1024);
+    int carve = (int)((100 * need + (size_t)smem_sm - 1) / (size_t)smem_sm);
+    carve = carve < 100 ? carve : 100;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve);
+    if (e != cudaSuccess) return e;
+    int fit = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, kBlock, 0);
+    if (e != cudaSuccess) return e;
+    per = fit < per ? fit : per;
+  }
   if (per < 1) return cudaErrorInvalidConfiguration;
   out->block = kBlock;
   out->grid = sms * per;
@@ -712,8 +783,12 @@ cudaError_t bfs_launch(const BfsParams &p, const LaunchGeom &g, cudaStream_t s) 
   const int grid =
       p.ctas_per_sm > 0 && p.ctas_per_sm < g.per_sm ? g.sms * p.ctas_per_sm : g.grid;
   void *args[] = {const_cast<BfsParams *>(&p)};
-  return cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(bfs_persistent_kernel),
-                                     dim3(grid), dim3(g.block), args, 0, s);
+  /* graphs with short out-lists run the instance with entry-aligned small
+   * levels; the others run the one compiled without them */
+  const void *fn = TBFS_SHORT_LEVELS && p.short_lists
+                       ? reinterpret_cast<const void *>(bfs_persistent_kernel<true>)
+                       : reinterpret_cast<const void *>(bfs_persistent_kernel<false>);
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(g.block), args, 0, s);
 }
 
 }  // namespace tbfs

@@ -59,53 +59,38 @@ __device__ __forceinline__ void smem_add_split(unsigned *lo, unsigned *hi, unsig
   if (new_h < old_h || (new_h >> 31) || add_h < xh) ovf = true;
 }
 
-#ifndef TBFS_BAR_GROUP
-#define TBFS_BAR_GROUP 0
-#endif
-
 /* Grid-wide barrier over a control block with fields bar (GridBarrier),
- * status and timeout_level.  Thread 0 of every CTA arrives; the last one to
- * arrive resets the counter and bumps the generation word, on which the
- * others wait.  With TBFS_BAR_GROUP > 0 the arrivals are two-level: CTAs
- * arrive on their group's counter (groups of TBFS_BAR_GROUP consecutive
- * CTAs), and only the last of each group arrives on the top counter, so no
- * one address takes more than max(group size, groups) arrivals.  Fences
- * before every arrival carry each CTA's writes along the chain to the
- * releasing store.  Every wait is bounded by timeout_ns of wall time
- * (globaltimer): on expiry the CTA records TBFS_ERR_TIMEOUT and returns
- * false, and so does every CTA that sees the error word set, so the kernel
- * always terminates.  `level` is recorded (+2) in timeout_level. */
+ * status and timeout_level.  Thread 0 of every CTA arrives with one atomic
+ * on a single counter and waits for the counter's top bit to flip: CTA 0
+ * adds 2^31 - (gridDim.x - 1) and every other CTA adds 1, so the barrier's
+ * arrivals add exactly 2^31 and the top bit changes only with the last one
+ * (the idea of the cooperative-groups grid barrier).  The counter needs no
+ * reset and no generation word, and a wait costs one fence, one atomic and
+ * the round trip of the poll that sees the flip -- a third of the chain of
+ * a counter that the last CTA resets before bumping a generation word.  A
+ * fence before the arrival releases the CTA's writes (made CTA-visible by
+ * the __syncthreads); the acquiring poll makes every CTA's writes visible
+ * after it.  The counter starts at 0 (control blocks are zeroed) and is
+ * back at 0 or 2^31 after every complete barrier.  Every wait is bounded
+ * by timeout_ns of wall time (globaltimer): on expiry the CTA records
+ * TBFS_ERR_TIMEOUT and returns false, and so does every CTA that sees the
+ * error word set, so the kernel always terminates (a CTA that left makes
+ * the others' next wait expire).  `level` is recorded (+2) in
+ * timeout_level. */
 template <class Ctl>
 __device__ bool grid_barrier(Ctl *ctl, long long timeout_ns, int level) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned gen = ld_acquire_u32(&ctl->bar.gen);
+    const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
     __threadfence();
-    bool last = false;
-    constexpr unsigned kGrp = TBFS_BAR_GROUP > 0 ? (unsigned)TBFS_BAR_GROUP : 1u;
-    if (TBFS_BAR_GROUP > 0 && gridDim.x > kGrp) {
-      const unsigned g = blockIdx.x / kGrp;
-      const unsigned groups = (gridDim.x + kGrp - 1) / kGrp;
-      const unsigned gsize = g + 1 < groups ? kGrp : gridDim.x - g * kGrp;
-      unsigned *gc = &ctl->bar.grp[g % tbfs::kBarGroups][0];
-      if (atomicAdd(gc, 1u) == gsize - 1) {
-        atomicExch(gc, 0u);
-        __threadfence();
-        last = atomicAdd(&ctl->bar.arrive, 1u) == groups - 1;
-      }
-    } else {
-      last = atomicAdd(&ctl->bar.arrive, 1u) == gridDim.x - 1;
-    }
-    if (last) {
-      atomicExch(&ctl->bar.arrive, 0u);
-      __threadfence();
-      st_release_u32(&ctl->bar.gen, gen + 1);
-    } else {
+    const unsigned old = atomicAdd(&ctl->bar.arrive, inc);
+    const unsigned want = (old & 0x80000000u) ^ 0x80000000u;
+    if (((old + inc) & 0x80000000u) != want) {
       const unsigned long long t0 = global_ns();
       unsigned spins = 0;
-      while (ld_acquire_u32(&ctl->bar.gen) == gen) {
+      while ((ld_acquire_u32(&ctl->bar.arrive) & 0x80000000u) != want) {
         if ((++spins & 31u) == 0) {
           if (ld_volatile(&ctl->status) != 0) {
             ok = 0;
@@ -119,9 +104,11 @@ __device__ bool grid_barrier(Ctl *ctl, long long timeout_ns, int level) {
           }
         }
       }
+    } else {
+      /* the last arrival: its atomic read every other arrival; the fence
+       * orders the CTA's next reads after them */
+      __threadfence();
     }
-    __threadfence();
-    if (ld_volatile(&ctl->status) != 0) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

@@ -41,16 +41,11 @@ inline cudaError_t dev_alloc(T **p, size_t bytes) {
   return dev_alloc(reinterpret_cast<void **>(p), bytes);
 }
 
-/* Words of the hand-written grid barrier (device_common.cuh): the top-level
- * arrival counter and the generation word on their own 128-byte lines, then
- * one arrival counter per group of CTAs, each on its own line. */
-constexpr int kBarGroups = 32; /* groups of up to TBFS_BAR_GROUP CTAs */
+/* Arrival counter of the hand-written grid barrier (device_common.cuh), on
+ * its own 128-byte line. */
 struct __align__(128) GridBarrier {
   unsigned arrive;
   unsigned pad0[31];
-  unsigned gen;
-  unsigned pad1[31];
-  unsigned grp[kBarGroups][32];
 };
 
 /* Device control block of one traversal; zeroed before every launch. */
@@ -98,7 +93,13 @@ struct BfsParams {
   /* bits of the largest in-degree (0: unknown); bounds the path counts'
    * growth per level (bfs_engine.cu) */
   int deg_bits;
+  /* nonzero: no out-list has more than kShortList entries, so small
+   * top-down levels may give every queue entry to one lane (bfs_engine.cu) */
+  int short_lists;
 };
+
+/* longest out-list for which a lane walks a whole list alone */
+constexpr int kShortList = 16;
 
 /* Launch geometry of the persistent kernel on the current device. */
 struct LaunchGeom {
@@ -109,6 +110,9 @@ struct LaunchGeom {
 
 cudaError_t bfs_launch(const BfsParams &p, const LaunchGeom &g, cudaStream_t s);
 cudaError_t bfs_geometry(int device, LaunchGeom *out);
+/* *out = the longest list of the n lists delimited by ptr[0..n] (ptr on the
+ * device), synchronously on the current device */
+cudaError_t longest_list(const int *ptr, int n, int *out);
 
 /* ---- frontier-matrix batch (batch_engine.cu) ----
  * Up to 256 roots on one graph advance together: bit r of a vertex's row
@@ -316,6 +320,7 @@ struct tbfs_graph {
   int *queues = nullptr; /* one allocation: q[3], e[3], a[3], n ints each */
   char *hot = nullptr;   /* one allocation: sigma_work, S_work, bitmaps */
   int deg_bits = 0;      /* bits of the largest in-degree */
+  bool short_lists = false; /* no out-list longer than kShortList */
   /* the caller's TBFS_GRAPH_SYMMETRIC (flags may also carry it when the
    * lists were found to equal their transpose on upload) */
   bool declared_symmetric = false;

@@ -180,6 +180,22 @@ void cache_store(const char *path, const std::string &key, const Tuned &t) {
 }
 
 }  // namespace
+
+cudaError_t longest_list(const int *ptr, int n, int *out) {
+  unsigned long long *dh = nullptr;
+  cudaError_t e = dev_alloc(&dh, kBuckets * sizeof(unsigned long long) + sizeof(int));
+  int *dm = reinterpret_cast<int *>(dh + kBuckets);
+  if (e == cudaSuccess) e = cudaMemset(dh, 0, kBuckets * sizeof(unsigned long long) + sizeof(int));
+  if (e == cudaSuccess) {
+    const int blocks = (int)std::min<long long>(((long long)n + 255) / 256, 4096);
+    degree_profile_kernel<<<blocks, 256>>>(ptr, n, dh, dm);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, dm, sizeof(int), cudaMemcpyDeviceToHost);
+  if (dh) dev_free(dh);
+  return e;
+}
+
 }  // namespace tbfs
 
 extern "C" tbfs_status tbfs_graph_degree_profile(tbfs_graph *g, int64_t *hist40,
