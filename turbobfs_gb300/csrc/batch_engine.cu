@@ -879,7 +879,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_BATCH_MINB) fm_bfs_kernel(const B
     else if (p.mode == TBFS_MODE_BOTTOM_UP)
       push = false;
     else
-      push = (double)qe * (double)p.alpha < (double)m_unseen + (double)kVCost * (double)n;
+      push = (float)qe * p.alpha < (float)m_unseen + (float)kVCost * (float)n;
     if (tid == 0 && p.trace && d < p.trace_cap - 1) {
       long long *rec = p.trace + 4 * (long long)d;
       rec[0] = (long long)dev::global_ns();

@@ -43,7 +43,9 @@
  * Direction rule (device side; Beamer, Asanovic, Patterson, "Direction-
  * optimizing breadth-first search", SC 2012): leave top-down when the
  * frontier's out-edges exceed (unexplored edges)/alpha; return to top-down
- * when the frontier shrinks below n/beta.
+ * when the frontier shrinks below n/beta.  The comparisons are in fp32:
+ * every thread evaluates them at every level, and fp64 issues slowly on
+ * this part (in fp64 they cost about 0.7 us per level).
  *
  * Memory model.  Queues and counters are read with ld.global.cg (L2).
  * Depth and path-count gathers use ordinary (L1-cacheable) loads: every
@@ -72,6 +74,9 @@
 #ifndef TBFS_SHORT_LEVELS
 #define TBFS_SHORT_LEVELS 1 /* small top-down levels of short-list graphs: a queue entry per lane */
 #endif
+#ifndef TBFS_SHORT_CAS_FIRST
+#define TBFS_SHORT_CAS_FIRST 1 /* aligned items claim with the CAS alone */
+#endif
 #ifndef TBFS_SPREAD_ITEMS
 #define TBFS_SPREAD_ITEMS 1 /* static work items round-robin over the CTAs */
 #endif
@@ -95,7 +100,7 @@ constexpr int kEPT = TBFS_EPT;     /* most consecutive edges per lane/round */
 /* queue entries per item of a small level of a short-list graph: at most
  * 8 * kShortList = 128 edges, one round of at most 4 per lane */
 constexpr unsigned kShortEntries = 8;
-constexpr double kBuWordCost = 4.0; /* a bitmap word of a bottom-up level, in list entries */
+constexpr float kBuWordCost = 4.0f; /* a bitmap word of a bottom-up level, in list entries */
 enum { DIR_TD = 0, DIR_BU = 1 };
 
 /* what an expansion does with path counts */
@@ -276,7 +281,23 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
       }
       int su[kEPT];   /* DISC: depth of the neighbour                        */
       unsigned in = 0; /* bit j: neighbour j is in the level the sigma mode needs */
-      if (DISC) {
+      /* an aligned item may claim with the CAS alone: its return value is
+       * the depth the plain read would have given */
+      constexpr bool cas_first = aligned && TBFS_SHORT_CAS_FIRST;
+      int ad[kEPT], dg[kEPT];
+      if (DISC && cas_first) {
+#pragma unroll
+        for (int j = 0; j < kEPT; ++j) {
+          su[j] = -2;
+          ad[j] = 0;
+          dg[j] = 0;
+          if ((valid >> j) & 1u) {
+            su[j] = atomicCAS(p.S + u[j], -1, d + 1);
+            ad[j] = __ldg(p.rp + u[j]);
+            dg[j] = __ldg(p.rp + u[j] + 1) - ad[j];
+          }
+        }
+      } else if (DISC) {
 #pragma unroll
         for (int j = 0; j < kEPT; ++j) su[j] = ((valid >> j) & 1u) ? p.S[u[j]] : -2;
         if (SIG == SIG_PULL) {
@@ -298,25 +319,36 @@ __device__ __forceinline__ void expand_chunk(const BfsParams &p, int d, int tgt,
       unsigned hit = 0; /* PUSH_NEW: targets at depth d+1 after this edge */
       if (DISC) {
         unsigned take = 0;
+        if (cas_first) {
 #pragma unroll
-        for (int j = 0; j < kEPT; ++j) {
-          if (su[j] == -1) {
-            const int old = atomicCAS(p.S + u[j], -1, d + 1);
-            if (old == -1) take |= 1u << j;
-            else if (old == d + 1) hit |= 1u << j;
-          } else if (su[j] == d + 1) {
-            hit |= 1u << j;
+          for (int j = 0; j < kEPT; ++j) {
+            if (su[j] == -1) take |= 1u << j;
+            else if (su[j] == d + 1) hit |= 1u << j;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < kEPT; ++j) {
+            if (su[j] == -1) {
+              const int old = atomicCAS(p.S + u[j], -1, d + 1);
+              if (old == -1) take |= 1u << j;
+              else if (old == d + 1) hit |= 1u << j;
+            } else if (su[j] == d + 1) {
+              hit |= 1u << j;
+            }
           }
         }
         hit |= take;
-        int dg[kEPT], ad[kEPT];
 #pragma unroll
         for (int j = 0; j < kEPT; ++j) {
-          ad[j] = 0;
-          dg[j] = 0;
+          if (!cas_first) {
+            ad[j] = 0;
+            dg[j] = 0;
+          }
           if ((take >> j) & 1u) {
-            ad[j] = __ldg(p.rp + u[j]);
-            dg[j] = __ldg(p.rp + u[j] + 1) - ad[j];
+            if (!cas_first) {
+              ad[j] = __ldg(p.rp + u[j]);
+              dg[j] = __ldg(p.rp + u[j] + 1) - ad[j];
+            }
             atomicOr(nb + ((unsigned)u[j] >> 5), 1u << ((unsigned)u[j] & 31u));
           }
         }
@@ -602,9 +634,9 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
       /* a bottom-up level also visits every vertex's bitmap word: without
        * that term, the tail of a deep graph (few unexplored edges left)
        * switched to bottom-up levels three times as costly as top-down ones */
-      if ((double)qe * (double)p.alpha > (double)m_u + kBuWordCost * (double)nwords) dir = DIR_BU;
+      if ((float)qe * p.alpha > (float)m_u + kBuWordCost * (float)nwords) dir = DIR_BU;
       else m_u -= qe;
-    } else if (qn < prev_qn && (double)qn <= (double)p.n / (double)p.beta) {
+    } else if (qn < prev_qn && (float)qn * p.beta <= (float)p.n) {
       dir = DIR_TD;
     }
     if (gtid == 0 && p.trace && d < p.trace_cap - 1) {
@@ -650,7 +682,7 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
     } else {
       ++bu;
       if (want_sigma && !sig_ready) { /* sigma(F_d): pull unless push reads far less */
-        if (p.symmetric && (double)qe <= (double)p.pull_ratio * (double)prev_qe)
+        if (p.symmetric && (float)qe <= p.pull_ratio * (float)prev_qe)
           A.kind = EX_PULL;
         else
           A = {EX_PUSH_AT, d, Qp, bm_cur, {1, 1, 0}, true};
@@ -664,29 +696,31 @@ __global__ void __launch_bounds__(kBlock, TBFS_MIN_BLOCKS) bfs_persistent_kernel
         A.chk = !ovf_seen && !(p.deg_bits > 0 && nb_next <= 63);
       if (A.kind == EX_PUSH_AT) A.chk = !ovf_seen && !(p.deg_bits > 0 && sig_bits <= 63);
     }
-    if (A.kind != EX_NONE) A.pl = plan_expand(A.Q.qe, nwarps, max_ept);
-    if (B.kind != EX_NONE) B.pl = plan_expand(B.Q.qe, nwarps, max_ept);
-    const unsigned n_tiles = dir == DIR_BU ? (nwords + kBuWords - 1) / kBuWords : 0u;
-    const unsigned n_a = A.pl.nch, n_ab = n_a + B.pl.nch, n_all = n_ab + n_tiles;
-    unsigned *wctr = &ctl->work[d & 3];
-    const int lane = threadIdx.x & 31;
-    /* work items: the first statically (global warp index), the rest from
-     * the level's counter past the static range, so that a small level
-     * costs no same-address atomics */
-    /* static items go round-robin over the CTAs (item i to CTA i % grid),
-     * so that a small level's work spreads over as many SMs as it has
-     * items instead of filling the first CTAs' warps */
-    unsigned item = TBFS_SPREAD_ITEMS ? (threadIdx.x >> 5) * gridDim.x + blockIdx.x
-                                      : blockIdx.x * kWarps + (threadIdx.x >> 5);
     /* a small top-down level of a graph with short lists: items of
-     * kShortEntries queue entries each, no owner search (expand_chunk) */
+     * kShortEntries queue entries each, no owner search (expand_chunk) and
+     * no edge-chunk plan */
     const bool short_level = SHORT && B.kind == EX_NONE &&
                              (A.kind == EX_DISC || A.kind == EX_DISC_PUSH_NEW) &&
                              qn <= kShortEntries * nwarps;
+    if (!short_level) {
+      if (A.kind != EX_NONE) A.pl = plan_expand(A.Q.qe, nwarps, max_ept);
+      if (B.kind != EX_NONE) B.pl = plan_expand(B.Q.qe, nwarps, max_ept);
+    }
+    const unsigned n_tiles = dir == DIR_BU ? (nwords + kBuWords - 1) / kBuWords : 0u;
+    const unsigned n_a = short_level ? 0u : A.pl.nch;
+    const unsigned n_ab = n_a + B.pl.nch, n_all = n_ab + n_tiles;
+    unsigned *wctr = &ctl->work[d & 3];
+    const int lane = threadIdx.x & 31;
+    /* work items: the first statically (one per warp), the rest from the
+     * level's counter past the static range, so that a small level costs
+     * no same-address atomics.  Static items go round-robin over the CTAs
+     * (item i to CTA i % grid), so that a small level's work spreads over
+     * as many SMs as it has items instead of filling the first CTAs' warps */
+    unsigned item = TBFS_SPREAD_ITEMS ? (threadIdx.x >> 5) * gridDim.x + blockIdx.x
+                                      : blockIdx.x * kWarps + (threadIdx.x >> 5);
     if (short_level) {
       const unsigned first = item * kShortEntries;
       if (first < qn) run_short_item(p, d, A, first, max_ept, nx, bm_next, win, ovf);
-      item = n_all; /* done */
     }
     while (item < n_all) {
       if (item < n_a) run_expand_item(p, d, A, item, nx, bm_next, win, ovf);
