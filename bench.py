@@ -497,6 +497,9 @@ def summary(line):
     gr = line.get("grid", {}).get("auto")
     if gr:
         out["grid_us_per_level"] = round(gr["us_per_level"], 2)
+    gt = line.get("grid", {}).get("autotuned")
+    if gt:
+        out["grid_us_per_level_autotuned"] = round(gt["us_per_level"], 2)
     return out
 
 
@@ -1147,6 +1150,21 @@ def grid_report(args):
             out[mode] = {"ms_per_bfs": float(np.mean(ms)), "levels": int(np.mean(lv)),
                          "us_per_level": float(1e3 * np.sum(ms) / np.sum(lv)),
                          "gteps": float(np.sum(ed) / np.sum(ms) / 1e6)}
+        # the engine shape and direction parameters tuned for this graph's
+        # degree profile (CTAs per SM above all: small levels are latency-bound)
+        kw = {k: v for k, v in g.autotune(roots[:1]).items() if k != "from_cache"}
+        g.bfs(int(roots[0]), **kw)  # warm
+        ms, lv = [], []
+        for r, (S, sg, ovf, _) in zip(roots, want):
+            res = g.bfs(int(r), **kw)
+            ms.append(res.stats["device_ms"])
+            lv.append(res.stats["levels"])
+            ok = ovf == 0
+            same &= bool(np.array_equal(res.S, S) and np.array_equal(res.sigma[ok], sg[ok]))
+        out["autotuned"] = {"ms_per_bfs": float(np.mean(ms)), "levels": int(np.mean(lv)),
+                            "us_per_level": float(1e3 * np.sum(ms) / np.sum(lv)),
+                            "params": {k: (round(v, 3) if isinstance(v, float) else v)
+                                       for k, v in kw.items()}}
     # the reference's entry points: graph built from the host arrays in every call
     n, nz = h.n, int(h.nnz)
     J = np.repeat(np.arange(n, dtype=np.int32), np.diff(h.col_ptr))
