@@ -203,18 +203,42 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+KERNEL_SOURCES = ["turbobfs_gb300/csrc/bfs_engine.cu", "turbobfs_gb300/csrc/device_common.cuh",
+                  "turbobfs_gb300/csrc/tbfs_internal.h"]
+
+
+def kernel_source_hash() -> str:
+    """sha256 over the single-source kernel's sources, in a fixed order."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        h.update((ROOT / rel).read_bytes())
+    return h.hexdigest()
+
+
 def traffic_per_launch(scale: int):
-    """dram bytes (read + write) per traversal from the committed ncu summary."""
+    """dram bytes (read + write) per traversal from the committed ncu summary,
+    with a note; None when the summary is absent or was measured on other
+    kernel sources (its kernel_source_sha256 line differs from the sources
+    built here)."""
     f = ROOT / "profiles" / f"bfs_persistent_kernel_rmat{scale}.md"
     if not f.exists():
-        return None
+        return None, f"no profiles/{f.name}"
+    traffic, sha = None, None
     for line in f.read_text().splitlines():
         if line.startswith("traffic_bytes_per_launch:"):
             try:
-                return int(line.split(":", 1)[1].strip())
+                traffic = int(line.split(":", 1)[1].strip())
             except ValueError:
-                return None
-    return None
+                traffic = None
+        if line.startswith("kernel_source_sha256:"):
+            sha = line.split(":", 1)[1].strip()
+    if traffic is None:
+        return None, f"profiles/{f.name} holds no traffic line"
+    if sha != kernel_source_hash():
+        return None, f"profiles/{f.name} was measured on other kernel sources"
+    return traffic, f"ncu dram bytes of one launch, profiles/{f.name} (same kernel sources)"
 
 
 def run_reference(args, world, rank):
@@ -391,7 +415,7 @@ def run_tbfs(args, world, rank, local):
     mean_launch_ms = float(np.mean(launch_ms))
     achieved = mean_bytes / (mean_launch_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = traffic_per_launch(args.scale)
+    traffic, traffic_note = traffic_per_launch(args.scale)
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -414,7 +438,7 @@ def run_tbfs(args, world, rank, local):
                                        "td_bu_levels_root0": [per_root[0]["td_levels"],
                                                               per_root[0]["bu_levels"]]}),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_note": traffic_note,
                      "kernel": "bfs_persistent_kernel",
                      "algorithmic_bytes_per_launch": mean_bytes,
                      "mean_launch_ms": mean_launch_ms,
