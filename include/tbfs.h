@@ -78,7 +78,7 @@ typedef struct tbfs_options {
   /* Path counts of a level found bottom-up are finished one level later,
    * either by pulling over that level's lists or by pushing from the
    * previous level's lists; pull is used unless it reads more than
-   * pull_ratio times as many list entries as push.  <= 0: default 4. */
+   * pull_ratio times as many list entries as push.  <= 0: default 1. */
   float pull_ratio;
   /* Engine shape of the single-source traversal (tbfs_autotune sets both):
    * the most list entries a lane handles per round of a push or pull (1..6;
@@ -97,7 +97,10 @@ typedef struct tbfs_stats {
   double device_ms;        /* CUDA-event time of the traversal on the stream */
 } tbfs_stats;
 
-/* Defaults: AUTO, want_sigma = 1, host outputs, alpha = 15, beta = 18. */
+/* Defaults: AUTO, want_sigma = 1, host outputs, alpha = 15, beta = 2,
+ * pull_ratio = 1 (near the best of RMAT scale 18-22 and Erdos-Renyi scale 22
+ * with path counts; Beamer's beta = 18 kept bottom-up levels after the
+ * frontier had begun to shrink, 14-43 % slower on those graphs). */
 void tbfs_options_init(tbfs_options *opt);
 
 /* Upload a CSC adjacency (col_ptr[n+1], row_idx[nnz], int32, 0-based).

@@ -60,7 +60,7 @@ def test_version_and_status_strings():
 def test_options_layout_and_defaults():
     o = tb.make_options()
     assert ctypes.sizeof(_lib.Options) == 64 and ctypes.sizeof(_lib.Stats) == 40
-    assert o.mode == 0 and o.want_sigma == 1 and o.alpha == 15.0 and o.beta == 18.0
+    assert o.mode == 0 and o.want_sigma == 1 and o.alpha == 15.0 and o.beta == 2.0 and o.pull_ratio == 1.0
 
 
 @pytest.mark.skipif(tb.device_count() > 0, reason="checks behaviour without a GPU")

@@ -82,8 +82,8 @@ extern "C" void tbfs_options_init(tbfs_options *opt) {
   opt->mode = TBFS_MODE_AUTO;
   opt->want_sigma = 1;
   opt->alpha = 15.0f;
-  opt->beta = 18.0f;
-  opt->pull_ratio = 4.0f;
+  opt->beta = 2.0f;
+  opt->pull_ratio = 1.0f;
 }
 
 extern "C" tbfs_status tbfs_host_alloc_pinned(size_t bytes, void **ptr) {
@@ -643,8 +643,8 @@ static tbfs_options resolve_opts(const tbfs_options *in) {
   tbfs_options_init(&o);
   if (in) o = *in;
   if (o.alpha <= 0.0f) o.alpha = 15.0f;
-  if (o.beta <= 0.0f) o.beta = 18.0f;
-  if (!(o.pull_ratio > 0.0f)) o.pull_ratio = 4.0f;
+  if (o.beta <= 0.0f) o.beta = 2.0f;
+  if (!(o.pull_ratio > 0.0f)) o.pull_ratio = 1.0f;
   return o;
 }
 

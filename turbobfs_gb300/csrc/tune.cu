@@ -146,7 +146,7 @@ std::string profile_key(const tbfs_graph *g, const int64_t *hist, int64_t maxd) 
 
 /* a cache line: "key alpha beta pull_ratio [max_ept ctas_per_sm]" */
 struct Tuned {
-  float a = 15.0f, b = 18.0f, pr = 4.0f;
+  float a = 15.0f, b = 2.0f, pr = 1.0f;
   int ept = 0, ctas = 0;
 };
 
