@@ -108,6 +108,7 @@ struct tbfs_arena {
   bool symmetric = false;
   std::vector<int32_t> n;
   std::vector<int64_t> nnz, voff, eoff; /* vertex / entry offsets of graph i */
+  std::vector<int> deg_bits;           /* bits of graph i's largest in-degree */
   int64_t nv = 0, ne = 0;
   int *cp = nullptr, *ic = nullptr, *rp = nullptr, *jr = nullptr; /* packed */
   unsigned char *work = nullptr; /* per-graph traversal blocks */
@@ -158,11 +159,17 @@ static tbfs_status arena_build(tbfs_arena *a, const int32_t *col_ptr, const int3
       tbfs_set_error("tbfs_arena_create: graph %d: col_ptr must start at 0 and end at nnz", i);
       return TBFS_ERR_INVALID_ARG;
     }
-    for (int32_t v = 0; v < n; ++v)
+    int32_t maxd = 0;
+    for (int32_t v = 0; v < n; ++v) {
       if (cp[v + 1] < cp[v]) {
         tbfs_set_error("tbfs_arena_create: graph %d: col_ptr decreases at %d", i, v);
         return TBFS_ERR_INVALID_ARG;
       }
+      maxd = std::max(maxd, cp[v + 1] - cp[v]);
+    }
+    int b = 0;
+    while (b < 31 && (1 << b) <= maxd) ++b; /* maxd < 2^b */
+    a->deg_bits.push_back(b);
     for (int64_t k = 0; k < a->nnz[i]; ++k)
       if (ic[k] < 0 || ic[k] >= n) {
         tbfs_set_error("tbfs_arena_create: graph %d: row index out of range", i);
@@ -307,6 +314,7 @@ extern "C" tbfs_status tbfs_arena_bfs(tbfs_arena *a, const int32_t *roots, const
       D.inv = nullptr;
       D.nnz = a->nnz[(size_t)i];
       D.n = a->n[(size_t)i];
+      D.deg_bits = a->deg_bits[(size_t)i];
       D.root = roots[i];
       carve(a->work + a->woff[(size_t)i], D.n, want_sigma, D);
       MTRY(cudaMemsetAsync(D.S, 0xff, (size_t)D.n * sizeof(int), s), "clear S");
@@ -651,6 +659,7 @@ tbfs_status server_step(tbfs_server *sv, bool *idle) {
     D.inv = r.g->inv;
     D.nnz = r.g->nnz;
     D.n = r.g->n;
+    D.deg_bits = r.g->deg_bits;
     D.root = r.root;
     carve(sv->mem + sl.off, D.n, r.sigma != nullptr, D);
     MTRY(cudaMemsetAsync(D.S, 0xff, (size_t)D.n * sizeof(int), s), "clear S");

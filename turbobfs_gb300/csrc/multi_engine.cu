@@ -102,14 +102,16 @@ __device__ __forceinline__ unsigned lane_owner(const unsigned *e, unsigned cnt, 
 }
 
 __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) {
+  constexpr int kWarps = kBlock / 32;
   __shared__ unsigned s_pre[kMultiMaxSlots + 1]; /* item prefix over slots      */
   __shared__ int s_d[kMultiMaxSlots];            /* level each slot runs next   */
   __shared__ unsigned s_qn[kMultiMaxSlots], s_qe[kMultiMaxSlots];
-  __shared__ unsigned s_part[kBlock];
-  __shared__ int s_active;
+  __shared__ unsigned long long s_wsum[kWarps];  /* per-warp edge sums          */
+  __shared__ int s_wact[kWarps];
+  __shared__ unsigned s_wscan[kWarps];           /* per-warp item sums          */
   InstDesc *I = P.inst;
   const int ns = P.nslots;
-  const int t = threadIdx.x, lane = t & 31;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const long long tid = (long long)blockIdx.x * kBlock + t;
   MultiCtl *ctl = P.ctl;
 
@@ -118,10 +120,12 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
 
   unsigned ph = 0;
   for (; ph < (unsigned)P.max_phases; ++ph) {
+    /* the host's "request waiting" flag (mapped host memory, a slow read):
+     * issued now, used at the end of the level */
+    int wake_now = 0;
+    if (tid == 0 && P.wake) wake_now = *P.wake;
     /* ---- plan: identical in every CTA (reads counters finished before the
-     * last barrier) ---- */
-    if (t == 0) s_active = 0;
-    __syncthreads();
+     * last barrier); block sums and scans by warp shuffles ---- */
     constexpr int kPer = (kMultiMaxSlots + kBlock - 1) / kBlock;
     unsigned qes[kPer];
     unsigned long long esum = 0;
@@ -156,21 +160,29 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
         }
       }
     }
-    /* rounds per item: enough items for every warp on small levels */
-    s_part[t] = (unsigned)min(esum, 0xffffffffull);
-    if (act) s_active = 1;
     if (fin && P.stop_on_done) ctl->stop[ph & 1u] = 1; /* CTA 0 only; read after the barrier */
-    __syncthreads();
-    for (int o = kBlock / 2; o > 0; o >>= 1) {
-      if (t < o) s_part[t] = (unsigned)min((unsigned long long)s_part[t] + s_part[t + o],
-                                           0xffffffffull);
-      __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(FULL, esum, o);
+    const int wact = __any_sync(FULL, act);
+    if (lane == 0) {
+      s_wsum[wid] = esum;
+      s_wact[wid] = wact;
     }
-    const unsigned nwarps = gridDim.x * (kBlock / 32);
-    const unsigned long long per_warp = s_part[0] / ((unsigned long long)kRoundEdges * nwarps);
+    __syncthreads();
+    unsigned long long etot = 0;
+    int any_act = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      etot += s_wsum[w];
+      any_act |= s_wact[w];
+    }
+    if (!any_act) break;
+    /* rounds per item: enough items for every warp on small levels */
+    const unsigned nwarps = gridDim.x * kWarps;
+    const unsigned long long per_warp =
+        min(etot, 0xffffffffull) / ((unsigned long long)kRoundEdges * nwarps);
     const unsigned rounds = (unsigned)max(1ull, min((unsigned long long)kMaxRounds, per_warp));
     const unsigned iedges = kRoundEdges * rounds;
-    __syncthreads();
     unsigned items[kPer];
     unsigned sum = 0;
 #pragma unroll
@@ -178,32 +190,38 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
       items[j] = (qes[j] + iedges - 1) / iedges;
       sum += items[j];
     }
-    s_part[t] = sum;
-    __syncthreads();
-    /* exclusive scan of the per-thread sums */
-    for (int o = 1; o < kBlock; o <<= 1) {
-      const unsigned x = t >= o ? s_part[t - o] : 0u;
-      __syncthreads();
-      s_part[t] += x;
-      __syncthreads();
+    /* exclusive scan of the per-thread sums: within the warp by shuffles,
+     * across the warps from their totals */
+    unsigned inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned x = __shfl_up_sync(FULL, inc, o);
+      if (lane >= o) inc += x;
     }
-    unsigned run = s_part[t] - sum;
+    if (lane == 31) s_wscan[wid] = inc;
+    __syncthreads();
+    unsigned wbase = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      const unsigned v = s_wscan[w];
+      if (w < wid) wbase += v;
+      total += v;
+    }
+    unsigned run = wbase + inc - sum;
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
       const int i = t * kPer + j;
       if (i < ns) s_pre[i] = run;
       run += items[j];
     }
-    if (t == kBlock - 1) s_pre[ns] = s_part[t];
+    if (t == 0) s_pre[ns] = total;
     __syncthreads();
-    if (!s_active) break;
-    const unsigned total = s_pre[ns];
     if (tid == 0) ctl->work[(ph + 2) & 3u] = 0u;
 
     /* ---- claim items: the first one statically (global warp index), the
      * rest from the phase's counter, so that a level with few items costs
      * no same-address atomics ---- */
-    unsigned it = blockIdx.x * (kBlock / 32) + (t >> 5);
+    unsigned it = (unsigned)wid * gridDim.x + blockIdx.x; /* round-robin over the CTAs */
     for (;; ) {
       if (it >= total) break;
       /* slot of the item: largest i with s_pre[i] <= it */
@@ -227,6 +245,12 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
       const int *rp = D.rp, *jr = D.jr;
       int *S = D.S;
       unsigned long long *sig = D.sig;
+      /* counts of level d+1 have at most 1 + (d+1) deg_bits bits: below 64
+       * they cannot overflow, and neither need be checked once the
+       * instance's overflow is recorded; such adds are reductions whose old
+       * value nobody waits for */
+      const bool chk = sig && !(D.deg_bits > 0 && 1 + (long long)(d + 1) * D.deg_bits <= 63) &&
+                       __ldcg(&D.ovf) == 0;
       const unsigned t0 = (it - s_pre[i]) * iedges;
       bool ovf = false;
       unsigned o0 = 0xffffffffu; /* owner of the round's first edge, once known */
@@ -325,9 +349,13 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
           for (int k = 0; k < kEPT; ++k) {
             if (tk[k] < qe && sv[k] == d + 1) {
               const unsigned long long x = su[k];
-              const unsigned long long old = atomicAdd(sig + v[k], x);
-              const unsigned long long s2 = old + x;
-              if (s2 < old || (s2 >> 63)) ovf = true;
+              if (chk) {
+                const unsigned long long old = atomicAdd(sig + v[k], x);
+                const unsigned long long s2 = old + x;
+                if (s2 < old || (s2 >> 63)) ovf = true;
+              } else {
+                atomicAdd(sig + v[k], x); /* result unused: a reduction */
+              }
             }
           }
         }
@@ -341,7 +369,7 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
       it = __shfl_sync(FULL, nx, 0);
     }
     /* a waiting request (host flag) ends the launch after this level */
-    if (tid == 0 && P.wake && *P.wake) ctl->stop[ph & 1u] = 1;
+    if (tid == 0 && wake_now) ctl->stop[ph & 1u] = 1;
     if (!grid_barrier(ctl, P.timeout_ns, (int)ph)) return;
     for (int i = t; i < ns; i += kBlock)
       if (s_qn[i]) s_d[i] += 1;

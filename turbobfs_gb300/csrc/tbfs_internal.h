@@ -218,6 +218,8 @@ struct InstDesc {
   int done;                   /* 1: finished (or an empty slot)                */
   int levels;
   int ovf;                    /* a path count reached 2^63                     */
+  int deg_bits;               /* bits of the largest in-degree (0: unknown):
+                                 counts of level d have at most 1 + d deg_bits */
   long long visited, edges;
 };
 
