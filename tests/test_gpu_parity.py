@@ -147,6 +147,36 @@ def test_compat_td_cooc(gpu_available, name):
         assert np.array_equal(_bits(sg[small]), _bits(fx.get("cooc_sigma", i)[small]))
 
 
+def test_compat_cooc_native_and_sorted_paths(gpu_available):
+    """bfs_gpu_td_cooc_sc runs straight over the pairs for graphs of at most
+    32 levels and sorts them into CSC beyond: a directed shallow graph and a
+    2 x 3000 ladder (3000 levels) in both directions, pairs in random order,
+    equal to the oracle's emulation of the reference's COOC driver (float
+    sigma; counts here stay below 2^24).  Out-of-range pairs are an error."""
+    rng = np.random.default_rng(11)
+    n = 20000
+    src = rng.integers(0, n, 80000, dtype=np.int32)
+    dst = rng.integers(0, n, 80000, dtype=np.int32)
+    n2 = 3000
+    a = np.arange(n2 - 1, dtype=np.int32)
+    lsrc = np.concatenate([a, a + n2, np.arange(n2, dtype=np.int32)])
+    ldst = np.concatenate([a + 1, a + 1 + n2, np.arange(n2, dtype=np.int32) + n2])
+    cases = [("directed", n, src, dst, (0, 5, 1234)),
+             ("ladder", 2 * n2, np.concatenate([lsrc, ldst]), np.concatenate([ldst, lsrc]), (0, 2500))]
+    for name, nv, I, J, roots in cases:
+        perm = rng.permutation(I.shape[0])
+        I = np.ascontiguousarray(I[perm], np.int32)
+        J = np.ascontiguousarray(J[perm], np.int32)
+        for r in roots:
+            sg = np.full(nv, -1.0, np.float32)
+            assert tb.bfs_gpu_td_cooc_sc(I, J, sg, r, I.shape[0], nv, 1) == 0, name
+            want = oracle.gpu_td_cooc(I, J, nv, r)
+            assert np.array_equal(_bits(sg), _bits(want)), (name, r)
+    bad = np.array([0, 1, 7], np.int32)
+    sg = np.zeros(5, np.float32)
+    assert tb.bfs_gpu_td_cooc_sc(bad, np.array([1, 2, 3], np.int32), sg, 0, 3, 5, 1) != 0
+
+
 # ------------------------------------------------------- synthetic sizes
 
 @pytest.mark.parametrize("kind,seed", [("er", 1), ("er", 2), ("rmat", 1), ("rmat", 2),

@@ -23,7 +23,7 @@ LIB = PKG / "libtbfs.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CU_SOURCES = ["bfs_engine.cu", "batch_engine.cu", "multi_engine.cu", "graph_ingest.cu", "api.cu",
               "batch_api.cu", "multi_api.cu", "brandes.cu", "tune.cu",
-              "noalloc.cu", "mm_ingest.cu", "devmem.cu", "validate.cu"]
+              "noalloc.cu", "mm_ingest.cu", "devmem.cu", "validate.cu", "cooc_engine.cu"]
 C_SOURCES = ["host_graph.c"]
 
 

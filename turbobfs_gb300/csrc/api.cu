@@ -962,6 +962,105 @@ int compat_grid(int n) {
   return (int)(b < 2432 ? (b > 0 ? b : 1) : 2432);
 }
 
+/* Levels a COOC call runs straight over the pairs before it sorts them
+ * into CSC instead (cooc_engine.cu): a level costs one pass over the pairs,
+ * the sort a few passes plus the degree grouping. */
+constexpr int kCoocMaxLevels = 32;
+
+/* The COOC entry point without the sort: upload the pairs, check them, run
+ * `reps` traversals over them, convert sigma to float into sig_h.  *done is
+ * false (and nothing is written) when the traversal needs more than
+ * kCoocMaxLevels levels. */
+tbfs_status cooc_native(const int *I_h, const int *J_h, int r, int nz, int n, int reps,
+                        float *sig_h, bool *done) {
+  *done = false;
+  tbfs_status st0 = need_device();
+  if (st0 != TBFS_OK) return st0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  tbfs::LaunchGeom geom;
+  if (e == cudaSuccess) e = tbfs::cooc_geometry(dev, &geom);
+  if (e != cudaSuccess) return cuda_fail(e, "cooc geometry", __LINE__);
+  const size_t nn = (size_t)n, m = nz > 0 ? (size_t)nz : 1, nwords = (nn + 31) / 32;
+  int *I = nullptr, *J = nullptr, *S = nullptr, *flag = nullptr;
+  unsigned long long *sg = nullptr;
+  float *out = nullptr;
+  unsigned *fb = nullptr;
+  tbfs::CoocCtl *ctl = nullptr;
+  e = tbfs::dev_alloc(&I, m * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&J, m * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&S, nn * sizeof(int));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&sg, nn * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&out, nn * sizeof(float));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&fb, 3 * nwords * sizeof(unsigned));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&ctl, sizeof(tbfs::CoocCtl));
+  if (e == cudaSuccess) e = tbfs::dev_alloc(&flag, sizeof(int));
+  if (e == cudaSuccess && nz > 0) e = cudaMemcpy(I, I_h, (size_t)nz * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && nz > 0) e = cudaMemcpy(J, J_h, (size_t)nz * sizeof(int), cudaMemcpyHostToDevice);
+  int bad = 0;
+  if (e == cudaSuccess) e = tbfs::cooc_check(I, J, nz, n, flag, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  tbfs_status st = TBFS_OK;
+  if (e != cudaSuccess) st = cuda_fail(e, "drop-in COOC upload", __LINE__);
+  else if (bad) st = invalid("bfs_gpu_td_cooc_sc: a row or column index is outside [0, n)");
+  tbfs::CoocParams p = {};
+  p.I = I;
+  p.J = J;
+  p.nnz = nz;
+  p.n = n;
+  p.root = r;
+  p.vec = ((reinterpret_cast<uintptr_t>(I) | reinterpret_cast<uintptr_t>(J)) & 15u) == 0;
+  p.max_levels = kCoocMaxLevels;
+  p.S = S;
+  p.sigma = sg;
+  for (int b = 0; b < 3; ++b) p.fb[b] = fb + (size_t)b * nwords;
+  p.ctl = ctl;
+  p.timeout_ns = 2000000000LL;
+  tbfs::CoocCtl c = {};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double total_ms = 0.0;
+  if (st == TBFS_OK) {
+    e = cudaEventCreate(&ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev1);
+  }
+  for (int i = 0; st == TBFS_OK && e == cudaSuccess && i < reps; ++i) {
+    e = cudaMemsetAsync(ctl, 0, sizeof(tbfs::CoocCtl), 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ev0, 0);
+    if (e == cudaSuccess) e = tbfs::cooc_launch(p, geom, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ev1, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(&c, ctl, sizeof(c), cudaMemcpyDeviceToHost);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+    total_ms += ms;
+    if (e == cudaSuccess && c.status != 0) {
+      tbfs_set_error("bfs_gpu_td_cooc_sc: grid barrier wait exceeded its budget at level %d",
+                     c.timeout_level - 2);
+      st = TBFS_ERR_TIMEOUT;
+    }
+    if (e == cudaSuccess && c.unfinished) break; /* deeper than the pass budget */
+  }
+  if (st == TBFS_OK && e == cudaSuccess && !c.unfinished) {
+    compat_td_kernel<<<compat_grid(n), 256>>>(nullptr, sg, out, n);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(sig_h, out, nn * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) *done = true;
+  }
+  if (st == TBFS_OK && e != cudaSuccess) st = cuda_fail(e, "drop-in COOC traversal", __LINE__);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  tbfs::dev_free(flag);
+  tbfs::dev_free(ctl);
+  tbfs::dev_free(fb);
+  tbfs::dev_free(out);
+  tbfs::dev_free(sg);
+  tbfs::dev_free(S);
+  tbfs::dev_free(J);
+  tbfs::dev_free(I);
+  if (st == TBFS_OK && *done && getenv("TBFS_PRINT_TIMES"))
+    printf("tbfs: levels = %d, r = %d, average time BFS = %lfms\n", c.levels, r, total_ms / reps);
+  return st;
+}
+
 /* Upload (CSC or COOC), run `repetition` traversals on the device (the last
  * one's result is kept, as the reference's drivers keep it), convert and
  * copy into the caller's S_h / sigma_h.  The graph is uploaded as general:
@@ -974,6 +1073,12 @@ int compat_run(const int *a, const int *b, bool cooc, int r, int nz, int n, int 
     return TBFS_ERR_INVALID_ARG;
   }
   const bool want_sigma = kind != K_BU;
+  if (kind == K_COOC) { /* shallow graphs: straight over the pairs, no sort */
+    bool done = false;
+    tbfs_status cs = cooc_native(a, b, r, nz, n, repetition < 1 ? 1 : repetition,
+                                 static_cast<float *>(sig_h), &done);
+    if (cs != TBFS_OK || done) return cs;
+  }
   tbfs_graph *g = nullptr;
   tbfs_status st = cooc ? tbfs_graph_create_cooc(a, b, n, nz, 0u, &g)
                         : tbfs_graph_create_csc(b, a, n, nz, 0u, &g);

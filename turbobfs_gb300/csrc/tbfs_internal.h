@@ -101,6 +101,31 @@ struct BfsParams {
 /* longest out-list for which a lane walks a whole list alone */
 constexpr int kShortList = 16;
 
+/* Control block of a COOC traversal (cooc_engine.cu); zeroed before every
+ * launch. */
+struct __align__(128) CoocCtl {
+  unsigned long long cnt[3]; /* vertices of level d in cnt[d % 3] */
+  int status, timeout_level;
+  int levels;
+  int sigma_overflow;
+  int unfinished;            /* gave up after max_levels levels */
+  int pad0[21];
+  GridBarrier bar;
+};
+
+struct CoocParams {
+  const int *I, *J;          /* entry k: edge I[k] -> J[k] */
+  long long nnz;
+  int n, root;
+  int vec;                   /* I and J 16-byte aligned: four pairs per load */
+  int max_levels;
+  int *S;
+  unsigned long long *sigma; /* null: depths only */
+  unsigned *fb[3];           /* frontier bitmaps, (n + 31) / 32 words each */
+  CoocCtl *ctl;
+  long long timeout_ns;
+};
+
 /* Launch geometry of the persistent kernel on the current device. */
 struct LaunchGeom {
   int grid = 0;
@@ -110,6 +135,11 @@ struct LaunchGeom {
 
 cudaError_t bfs_launch(const BfsParams &p, const LaunchGeom &g, cudaStream_t s);
 cudaError_t bfs_geometry(int device, LaunchGeom *out);
+cudaError_t cooc_geometry(int device, LaunchGeom *out);
+cudaError_t cooc_launch(const CoocParams &p, const LaunchGeom &g, cudaStream_t s);
+/* *d_flag = 1 when some I[k] or J[k] is outside [0, n) */
+cudaError_t cooc_check(const int *I, const int *J, long long nnz, int n, int *d_flag,
+                       cudaStream_t s);
 /* *out = the longest list of the n lists delimited by ptr[0..n] (ptr on the
  * device), synchronously on the current device */
 cudaError_t longest_list(const int *ptr, int n, int *out);
