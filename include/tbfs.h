@@ -82,7 +82,8 @@ typedef struct tbfs_options {
   float pull_ratio;
   /* Engine shape of the single-source traversal (tbfs_autotune sets both):
    * the most list entries a lane handles per round of a push or pull (1..6;
-   * 0 = 6), and CTAs per SM of the persistent launch (0 = as many as fit). */
+   * 0 = 6), and CTAs per SM of the persistent launch (0 = as many as fit,
+   * or 2 on graphs whose out-lists all have at most 16 entries). */
   int32_t max_ept;
   int32_t ctas_per_sm;
 } tbfs_options;

@@ -38,7 +38,7 @@ def test_autotune_candidates_cache_and_results(gpu_available, tmp_path):
         assert t1["alpha"] in (4.0, 6.0, 9.0, 12.0, 15.0, 24.0, 60.0)
         assert t1["beta"] in (1.0, 2.0, 4.0, 18.0)
         assert t1["pull_ratio"] in (0.5, 1.0, 2.0, 4.0)
-        assert t1["max_ept"] in (2, 4, 0) and t1["ctas_per_sm"] in (1, 2, 0)
+        assert t1["max_ept"] in (2, 4, 0) and t1["ctas_per_sm"] in (1, 2, 4, 0)
         t2 = g.autotune(roots, cache=cache)
         keys = ("alpha", "beta", "pull_ratio", "max_ept", "ctas_per_sm")
         assert t2["from_cache"] and all(t2[k] == t1[k] for k in keys)

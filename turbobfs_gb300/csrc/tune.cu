@@ -382,7 +382,7 @@ extern "C" tbfs_status tbfs_autotune(tbfs_graph *g, const int32_t *roots, int32_
   /* stage 1, the engine's shape at the default direction parameters: list
    * entries per lane and round, CTAs per SM */
   const int epts[] = {2, 4, 0};
-  const int ctass[] = {1, 2, 0};
+  const int ctass[] = {1, 2, 4}; /* 4 = every CTA that fits (0 means 2 on short-list graphs) */
   const tbfs::Tuned s0 = best;
   for (int e : epts)
     for (int c : ctass) {
