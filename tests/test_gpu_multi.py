@@ -73,6 +73,34 @@ def test_arena_directed_and_many_launches(gpu_available):
             _check_exact(gs[i], roots[i], Si, sgi, st[i])
 
 
+def test_arena_short_and_long_lists_in_one_launch(gpu_available):
+    """Deep low-degree instances share launches with shallow hub-heavy ones:
+    a grid, a 2 x 4000 ladder (4000 levels), directed graphs with
+    out-degrees up to 16 and with one of 17, and an RMAT graph; every one
+    equals the exact oracle."""
+    rng = np.random.default_rng(12)
+
+    def outdeg_graph(n, max_out, hub):
+        deg = rng.integers(0, max_out + 1, n)
+        if hub:
+            deg[1] = hub
+        src = np.repeat(np.arange(n, dtype=np.int32), deg)
+        return graphs.from_edges(n, src, rng.integers(0, n, src.size, dtype=np.int32))
+
+    n2 = 4000
+    a_ = np.arange(n2 - 1, dtype=np.int32)
+    lad = graphs.from_edges(2 * n2, np.concatenate([a_, a_ + n2, np.arange(n2, dtype=np.int32)]),
+                            np.concatenate([a_ + 1, a_ + 1 + n2, np.arange(n2, dtype=np.int32) + n2]),
+                            symmetrize=True)
+    gs = [graphs.grid(150, seed=5), lad, outdeg_graph(20000, 16, 0), outdeg_graph(20000, 16, 17),
+          graphs.rmat(12, 16, seed=5)]
+    roots = np.array([7, 0, 3, 1, 11], dtype=np.int32)
+    with tb.Arena(gs, symmetric=False) as a:
+        S, sg, st = a.bfs(roots)
+        for i, (Si, sgi) in enumerate(zip(a.split(S), a.split(sg))):
+            _check_exact(gs[i], roots[i], Si, sgi, st[i])
+
+
 def test_arena_overflow_flag(gpu_available):
     gs = [graphs.layered_bipartite(16, 17), graphs.layered_bipartite(16, 16), graphs.rmat(8, 8, seed=1)]
     with tb.Arena(gs) as a:
