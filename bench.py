@@ -736,7 +736,7 @@ def batched_report(args):
                          "peak": peak, "peak_source": f"{peak_kind} hbm_gbs",
                          "note": "the batch's own bytes: 12 k n of S and sigma written once plus "
                                  "one pass over col_ptr / row_idx; the kernels' measured DRAM "
-                                 "traffic is in profiles/launches_batched_report.md"},
+                                 "traffic is in profiles/fm_kernels_rmat19_256roots_traffic.md"},
             "per_root_bytes": {"bytes": per_root,
                                "gbs": per_root / (t_batch / 1e3) / 1e9,
                                "note": "sum over roots of 4 nnz_c + 8 n_c + 12 n, what k "
