@@ -101,7 +101,7 @@ __device__ __forceinline__ unsigned lane_owner(const unsigned *e, unsigned cnt, 
   return lo;
 }
 
-__global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) {
+__global__ void __launch_bounds__(kBlock, TBFS_MULTI_PER_SM) multi_bfs_kernel(const MultiParams P) {
   constexpr int kWarps = kBlock / 32;
   __shared__ unsigned s_pre[kMultiMaxSlots + 1]; /* item prefix over slots      */
   __shared__ int s_d[kMultiMaxSlots];            /* level each slot runs next   */
@@ -127,6 +127,31 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
     /* ---- plan: identical in every CTA (reads counters finished before the
      * last barrier); block sums and scans by warp shuffles ---- */
     constexpr int kPer = (kMultiMaxSlots + kBlock - 1) / kBlock;
+    /* every read of the plan in one round trip: the previous level's stop
+     * word, each slot's done flag and queue counter, and (CTA 0) the totals
+     * its bookkeeping adds to */
+    const bool stop_prev = ph > 0 && __ldcg(&ctl->stop[(ph - 1) & 1u]) != 0;
+    unsigned long long qvs[kPer];
+    long long vis[kPer], edg[kPer];
+    bool dns[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int i = t * kPer + j;
+      qvs[j] = 0ull;
+      vis[j] = edg[j] = 0;
+      dns[j] = true;
+      if (i < ns) {
+        dns[j] = __ldcg(&I[i].done) != 0;
+        qvs[j] = __ldcg(&I[i].ctr[s_d[i] % 3]);
+        if (blockIdx.x == 0) {
+          vis[j] = I[i].visited;
+          edg[j] = I[i].edges;
+        }
+      }
+    }
+    /* a stop requested during the previous level ends the launch before
+     * any bookkeeping of this one */
+    if (stop_prev) break;
     unsigned qes[kPer];
     unsigned long long esum = 0;
     int act = 0, fin = 0;
@@ -136,8 +161,8 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
       qes[j] = 0;
       if (i < ns) {
         const int d = s_d[i];
-        const bool done = __ldcg(&I[i].done) != 0;
-        const unsigned long long qv = done ? 0ull : __ldcg(&I[i].ctr[d % 3]);
+        const bool done = dns[j];
+        const unsigned long long qv = done ? 0ull : qvs[j];
         const unsigned qn = (unsigned)(qv >> 32), qe = (unsigned)qv;
         s_qn[i] = qn;
         s_qe[i] = qe;
@@ -151,8 +176,8 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
           if (qn) {
             I[i].ctr[(d + 2) % 3] = 0ull;
             I[i].levels = d + 1;
-            I[i].visited += qn;
-            I[i].edges += qe;
+            I[i].visited = vis[j] + qn;
+            I[i].edges = edg[j] + qe;
           } else {
             I[i].done = 1;
             fin = 1;
@@ -374,10 +399,6 @@ __global__ void __launch_bounds__(kBlock) multi_bfs_kernel(const MultiParams P) 
     for (int i = t; i < ns; i += kBlock)
       if (s_qn[i]) s_d[i] += 1;
     __syncthreads();
-    if (__ldcg(&ctl->stop[ph & 1u])) {
-      ++ph;
-      break;
-    }
   }
   /* the level each instance runs next, for the following launch */
   if (blockIdx.x == 0)
