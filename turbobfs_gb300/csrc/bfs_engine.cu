@@ -38,7 +38,12 @@
  * space) and the start of its list.  A warp takes a contiguous range of
  * flattened edges, stages 128 queue entries at a time in shared memory, and
  * every lane handles kEPT consecutive edges per round, so that many list
- * reads, then that many depth gathers, are in flight per lane.
+ * reads, then that many depth gathers, are in flight per lane.  On graphs
+ * whose out-lists are all short (kShortList entries at most) the kernel
+ * instance bfs_persistent_kernel<true> cuts small top-down levels into
+ * items of kShortEntries whole queue entries instead, which need no owner
+ * search (the chain of dependent L2 round trips is what a small level
+ * costs); other graphs run the instance compiled without that path.
  *
  * Direction rule (device side; Beamer, Asanovic, Patterson, "Direction-
  * optimizing breadth-first search", SC 2012): leave top-down when the
@@ -72,7 +77,7 @@
 #define TBFS_MIN_BLOCKS 4 /* 4 CTAs of 256 per SM: 64 registers (a small spill) */
 #endif
 #ifndef TBFS_SHORT_LEVELS
-#define TBFS_SHORT_LEVELS 1 /* small top-down levels of short-list graphs: a queue entry per lane */
+#define TBFS_SHORT_LEVELS 1 /* small top-down levels of short-list graphs: items of whole queue entries */
 #endif
 #ifndef TBFS_SHORT_CAS_FIRST
 #define TBFS_SHORT_CAS_FIRST 1 /* aligned items claim with the CAS alone */
